@@ -1,0 +1,839 @@
+// lg_api.cu -- C ABI of the LETKF analysis step (include/letkf_gpu.h).
+//
+// Host-side responsibilities:
+//   * the virtual block decomposition of the reference's DA ranks
+//     (pro_info_get_indx, x86/DA/utils/pro_info.F90:96-125) and each block's
+//     neighbour-block table (comm_info_init / nearest_dist,
+//     x86/DA/LETKF/src/letkf_init.F90:100-164, 288-341), computed once per grid;
+//   * the block observation lists that the Redis box query returns
+//     (redis_wrapper.c:4158-4296: inclusive %.5f-formatted lon/lat bounds,
+//     observations in index order), computed once per observation set;
+//   * the analysis pipeline on the device: H(x) -> selection (count, scan,
+//     fill) -> per-chunk Gram -> eigensolve + update, all on one stream.
+// Host code is compiled with -ffp-contract=off: the neighbour-block distances
+// are REAL(4) expressions whose rounding must not change by fusion.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "lg_internal.h"
+
+using lg::Geometry;
+
+struct lg_ctx {
+  lg_config cfg;
+  int dev = 0;
+  cudaStream_t own_stream = nullptr;
+  Geometry geo{};
+  int x_sec = 0, x_res = 0, y_sec = 0, y_res = 0;
+  std::vector<int4> blk;
+  std::vector<int> lat_block, lon_block, nb_off, nb_blk;
+  std::vector<float> glat, glon;
+  std::vector<int> var_start;
+  bool have_grid = false, have_obs = false;
+  // device geometry
+  float *d_glat = nullptr, *d_glon = nullptr;
+  double *d_ca = nullptr, *d_cb = nullptr;
+  int4* d_blk = nullptr;
+  int *d_lat_block = nullptr, *d_lon_block = nullptr, *d_nb_off = nullptr, *d_nb_blk = nullptr;
+  // observations
+  lg::TypeTable types{};
+  lg::ObsDev obs{};
+  std::vector<void*> obs_bufs;
+  std::vector<int> h_copy_obs, h_copy_block, h_copy_eoff;
+  // H(x)
+  lg::HxDev hx{};
+  size_t hx_entries_cap = 0;
+  // lists
+  lg::ListDev lists{};
+  size_t list_cap = 0;
+  void* d_scan_tmp = nullptr;
+  size_t scan_tmp_bytes = 0;
+  int64_t list_total = 0;
+  // solve workspace
+  double *d_C = nullptr, *d_t = nullptr;
+  size_t solve_cap = 0;
+  // status words: [0] err, [1] eig_fail
+  int* d_status = nullptr;
+  unsigned long long* d_band = nullptr;
+  // staging for host-array runs
+  double *d_xb = nullptr, *d_axb = nullptr, *d_xa = nullptr, *d_axa = nullptr;
+  size_t state_elems = 0;
+  lg_stats stats{};
+  cudaEvent_t ev[5] = {};
+};
+
+namespace {
+
+#define CK(call)                                                                     \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      fprintf(stderr, "letkf_gb300: %s failed: %s\n", #call, cudaGetErrorString(e_)); \
+      return LG_ERR_CUDA;                                                            \
+    }                                                                                \
+  } while (0)
+
+template <typename T>
+int dalloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return LG_ERR_NOMEM;
+  }
+  return LG_OK;
+}
+
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+// pro_info_get_indx: x = latitude blocks, y = longitude blocks, 1-based
+void get_indx(const lg_ctx* c, int bx, int by, int* tx_s, int* tx_e, int* ty_s, int* ty_e) {
+  if (bx - 1 < c->x_res) {
+    *tx_s = (bx - 1) * (c->x_sec + 1) + 1;
+    *tx_e = *tx_s + c->x_sec;
+  } else {
+    *tx_s = (bx - 1) * c->x_sec + c->x_res + 1;
+    *tx_e = *tx_s + c->x_sec - 1;
+  }
+  if (by - 1 < c->y_res) {
+    *ty_s = (by - 1) * (c->y_sec + 1) + 1;
+    *ty_e = *ty_s + c->y_sec;
+  } else {
+    *ty_s = (by - 1) * c->y_sec + c->y_res + 1;
+    *ty_e = *ty_s + c->y_sec - 1;
+  }
+}
+
+// latlon_dist_r8 on the host (pro_info.F90:149-161)
+double host_dist_r8(double x1, double y1, double x2, double y2) {
+  const double pi = (double)(atanf(1.0f) * 4.0f);
+  const double a = (double)6371.393f;
+  double v = cos(x1 / 180.0 * pi) * cos(x2 / 180.0 * pi) * cos(y1 / 180.0 * pi - y2 / 180.0 * pi) +
+             sin(x1 / 180.0 * pi) * sin(x2 / 180.0 * pi);
+  if (!(v < 1.0)) v = (v != v) ? v : 1.0;
+  return a * acos(v);
+}
+
+// latlon_dist_r4 (pro_info.F90:163-175)
+float host_dist_r4(float x1, float y1, float x2, float y2) {
+  const float pi = atanf(1.0f) * 4.0f;
+  float v = cosf(x1 / 180.0f * pi) * cosf(x2 / 180.0f * pi) * cosf(y1 / 180.0f * pi - y2 / 180.0f * pi) +
+            sinf(x1 / 180.0f * pi) * sinf(x2 / 180.0f * pi);
+  if (!(v < 1.0f)) v = (v != v) ? v : 1.0f;
+  return 6371.393f * acosf(v);
+}
+
+float GL(const lg_ctx* c, int i) { return c->glat[i - 1]; }
+float GN(const lg_ctx* c, int i) { return c->glon[i - 1]; }
+
+// nearest_dist (letkf_init.F90:288-341)
+double nearest_dist(const lg_ctx* c, int bx1, int by1, int bx2, int by2) {
+  int xs1, xe1, ys1, ye1, xs2, xe2, ys2, ye2, tx1, tx2;
+  get_indx(c, bx1, by1, &xs1, &xe1, &ys1, &ye1);
+  get_indx(c, bx2, by2, &xs2, &xe2, &ys2, &ye2);
+  if (bx1 > bx2) {
+    tx1 = xs1; tx2 = xe2 + 1;
+  } else if (bx1 < bx2) {
+    tx1 = xe1 + 1; tx2 = xs2;
+  } else if (bx1 > c->cfg.global_nx / 2) {
+    tx1 = xe1 + 1; tx2 = xe2 + 1;
+  } else {
+    tx1 = xs1; tx2 = xs2;
+  }
+  float lat1 = GL(c, tx1), lat2 = GL(c, tx2);
+  const double polar = c->cfg.obs_polar;
+  if (fabs((double)lat1) > polar) lat1 = (float)(lat1 >= 0.0f ? fabs(polar) : -fabs(polar));
+  if (fabs((double)lat2) > polar) lat2 = (float)(lat2 >= 0.0f ? fabs(polar) : -fabs(polar));
+  const int gy = c->cfg.num_lon;
+  if (by1 == by2) return (double)host_dist_r4(lat1, GN(c, ys1), lat2, GN(c, ys2));
+  float d1 = host_dist_r4(lat1, GN(c, ys1), lat2, GN(c, (ye2 % gy) + 1));
+  float d2 = host_dist_r4(lat1, GN(c, (ye1 % gy) + 1), lat2, GN(c, ys2));
+  return (double)(d1 < d2 ? d1 : d2);
+}
+
+// comm_info_init (letkf_init.F90:100-164): neighbour blocks in traversal order
+void neighbour_blocks(const lg_ctx* c, int bx, int by, std::vector<int>& out) {
+  const int gnx = c->cfg.global_nx, gny = c->cfg.global_ny;
+  const double L = c->cfg.local_dist;
+  int s_lat, e_lat, s_lon, e_lon, tx_s, tx_e, ty_s, ty_e;
+  get_indx(c, bx, by, &s_lat, &e_lat, &s_lon, &e_lon);
+  int north_n = 0, south_n = 0;
+  const double y1 = GN(c, s_lon), y2 = y1;
+  double x1 = GL(c, s_lat);
+  for (int tb = bx - 1; tb > 0; --tb) {
+    get_indx(c, tb, by, &tx_s, &tx_e, &ty_s, &ty_e);
+    if (host_dist_r8(x1, y1, (double)GL(c, tx_e + 1), y2) > L) break;
+    north_n++;
+  }
+  x1 = GL(c, e_lat + 1);
+  for (int tb = bx + 1; tb <= gnx; ++tb) {
+    get_indx(c, tb, by, &tx_s, &tx_e, &ty_s, &ty_e);
+    if (host_dist_r8(x1, y1, (double)GL(c, tx_s), y2) > L) break;
+    south_n++;
+  }
+  for (int i = -north_n; i <= south_n; ++i) {
+    const int tbx = bx + i;
+    int west_n = 0, east_n = 0, tby = by;
+    while (west_n <= (gny - 1) / 2) {
+      tby = ((tby + gny - 2) % gny) + 1;
+      if (nearest_dist(c, bx, by, tbx, tby) > L) break;
+      west_n++;
+    }
+    tby = by;
+    while (east_n <= (gny - 1) / 2) {
+      tby = (tby % gny) + 1;
+      if (nearest_dist(c, bx, by, tbx, tby) > L) break;
+      east_n++;
+    }
+    if (west_n + east_n > gny - 1) east_n--;
+    for (int j = -west_n; j <= east_n; ++j) {
+      const int nby = ((by + j - 1 + gny) % gny) + 1;
+      out.push_back((nby - 1) * gnx + (tbx - 1));
+    }
+  }
+}
+
+// %.5f-formatted box bound as the Redis server parses it
+double box_bound(float v) {
+  char buf[64];
+  snprintf(buf, sizeof buf, "%.5f", (double)v);
+  return strtod(buf, nullptr);
+}
+
+void free_obs(lg_ctx* c) {
+  for (void* p : c->obs_bufs) cudaFree(p);
+  c->obs_bufs.clear();
+  c->obs = lg::ObsDev{};
+  c->have_obs = false;
+}
+
+template <typename T>
+int upload(lg_ctx* c, const T* h, size_t n, const T** out) {
+  T* d = nullptr;
+  if (dalloc(&d, n) != LG_OK) return LG_ERR_NOMEM;
+  c->obs_bufs.push_back(d);
+  if (n) CK(cudaMemcpy(d, h, sizeof(T) * n, cudaMemcpyHostToDevice));
+  *out = d;
+  return LG_OK;
+}
+
+template <typename T>
+int scratch(lg_ctx* c, size_t n, T** out) {
+  T* d = nullptr;
+  if (dalloc(&d, n) != LG_OK) return LG_ERR_NOMEM;
+  c->obs_bufs.push_back(d);
+  *out = d;
+  return LG_OK;
+}
+
+int ensure_hx(lg_ctx* c, size_t entries) {
+  if (entries <= c->hx_entries_cap && c->hx.yb) return LG_OK;
+  dfree(c->hx.yb); dfree(c->hx.yb32); dfree(c->hx.dis); dfree(c->hx.lnp); dfree(c->hx.rdiag);
+  const size_t cap = entries + 1;
+  const size_t k = (size_t)c->cfg.ens;
+  int r = LG_OK;
+  r |= dalloc(&c->hx.yb, cap * k);
+  if (c->cfg.precision == LG_PREC_MIXED) r |= dalloc(&c->hx.yb32, cap * k);
+  r |= dalloc(&c->hx.dis, cap);
+  r |= dalloc(&c->hx.lnp, cap);
+  r |= dalloc(&c->hx.rdiag, cap);
+  if (r != LG_OK) return LG_ERR_NOMEM;
+  c->hx_entries_cap = cap;
+  return LG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lg_status_string(int s) {
+  switch (s) {
+    case LG_OK: return "LG_OK";
+    case LG_ERR_ARG: return "LG_ERR_ARG";
+    case LG_ERR_SHAPE: return "LG_ERR_SHAPE";
+    case LG_ERR_UNSUPPORTED: return "LG_ERR_UNSUPPORTED";
+    case LG_ERR_NAN: return "LG_ERR_NAN";
+    case LG_ERR_OBS_OUTSIDE: return "LG_ERR_OBS_OUTSIDE";
+    case LG_ERR_VARNAME: return "LG_ERR_VARNAME";
+    case LG_ERR_EIG: return "LG_ERR_EIG";
+    case LG_ERR_CUDA: return "LG_ERR_CUDA";
+    case LG_ERR_NOMEM: return "LG_ERR_NOMEM";
+    case LG_ERR_STATE: return "LG_ERR_STATE";
+    case LG_ERR_TIMEOUT: return "LG_ERR_TIMEOUT";
+    default: return "LG_ERR_UNKNOWN";
+  }
+}
+
+int lg_create(lg_ctx** out, const lg_config* cfg) {
+  if (!out || !cfg) return LG_ERR_ARG;
+  *out = nullptr;
+  const lg_config& g = *cfg;
+  if (g.ens < 2 || g.ens > 128 || g.num_lat < 1 || g.num_lon < 1 || g.nz < 1 || g.halo < 1 ||
+      g.n_var < 1 || g.n_var > LG_MAX_VARS || g.global_nx < 1 || g.global_ny < 1 ||
+      g.global_nx > g.num_lat || g.global_ny > g.num_lon || g.local_dist <= 0.0 ||
+      g.inflation <= 0.0 || g.ps_index < 1)
+    return LG_ERR_ARG;
+  if (g.cube_n != 1 || g.cube_nz != 1 || g.overlap != 0) return LG_ERR_UNSUPPORTED;
+  if (g.precision != LG_PREC_FP64 && g.precision != LG_PREC_MIXED) return LG_ERR_ARG;
+  int rows = 0;
+  for (int v = 0; v < g.n_var; ++v) {
+    if (g.var_lev[v] != 1 && g.var_lev[v] != g.nz) return LG_ERR_SHAPE;
+    rows += g.var_lev[v];
+  }
+  if (g.ps_index > rows) return LG_ERR_ARG;
+  lg_ctx* c = new lg_ctx();
+  c->cfg = g;
+  cudaGetDevice(&c->dev);
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return LG_ERR_CUDA;
+  }
+  for (auto& e : c->ev) cudaEventCreate(&e);
+  Geometry& geo = c->geo;
+  geo.ens = g.ens;
+  geo.num_lat = g.num_lat;
+  geo.num_lon = g.num_lon;
+  geo.nz = g.nz;
+  geo.halo = g.halo;
+  geo.n_var = g.n_var;
+  int cur = 0;
+  for (int v = 0; v < g.n_var; ++v) {
+    geo.var_start[v] = cur;
+    geo.var_lev[v] = g.var_lev[v];
+    cur += g.var_lev[v];
+  }
+  geo.n = cur;
+  geo.ps_row = g.ps_index - 1;
+  geo.vcoord = g.vcoord;
+  geo.local_dist = g.local_dist;
+  geo.vert_dist = g.vert_dist;
+  geo.inflation = g.inflation;
+  geo.obs_polar = g.obs_polar;
+  geo.gc_filter = g.gc_filter;
+  geo.gc_filter_vertical = g.gc_filter_vertical;
+  geo.max_obs = g.max_obs;
+  geo.global_nx = g.global_nx;
+  geo.global_ny = g.global_ny;
+  geo.nblocks = g.global_nx * g.global_ny;
+  // decomposition (module_da_parallel.F90:84-87 with pro_info_init's argument roles)
+  c->x_sec = g.num_lat / g.global_nx;
+  c->x_res = g.num_lat % g.global_nx;
+  c->y_sec = g.num_lon / g.global_ny;
+  c->y_res = g.num_lon % g.global_ny;
+  if (dalloc(&c->d_status, 4) != LG_OK || dalloc(&c->d_band, 1) != LG_OK) {
+    lg_destroy(c);
+    return LG_ERR_NOMEM;
+  }
+  *out = c;
+  return LG_OK;
+}
+
+int lg_set_grid(lg_ctx* c, const float* grid_lat, const float* grid_lon, const double* coef_a,
+                const double* coef_b, double p0, double ptop) {
+  if (!c || !grid_lat || !grid_lon || !coef_a) return LG_ERR_ARG;
+  if (c->cfg.vcoord == LG_VCOORD_HYBRID && !coef_b) return LG_ERR_ARG;
+  const lg_config& g = c->cfg;
+  c->glat.assign(grid_lat, grid_lat + g.num_lat + 1);
+  c->glon.assign(grid_lon, grid_lon + g.num_lon + 1);
+  c->glat[g.num_lat] = 90.0f;   // pro_info.F90:82-83
+  c->glon[g.num_lon] = 360.0f;
+  for (int i = 1; i < g.num_lat; ++i)
+    if (!(c->glat[i] > c->glat[i - 1])) return LG_ERR_ARG;
+  for (int i = 1; i < g.num_lon; ++i)
+    if (!(c->glon[i] > c->glon[i - 1])) return LG_ERR_ARG;
+  // blocks, column->block maps, neighbour tables
+  const int nb = g.global_nx * g.global_ny;
+  c->blk.assign(nb, int4{0, 0, 0, 0});
+  c->lat_block.assign(g.num_lat, 0);
+  c->lon_block.assign(g.num_lon, 0);
+  c->nb_off.assign(nb + 1, 0);
+  c->nb_blk.clear();
+  for (int by = 1; by <= g.global_ny; ++by)
+    for (int bx = 1; bx <= g.global_nx; ++bx) {
+      const int b = (by - 1) * g.global_nx + (bx - 1);
+      int s0, e0, s1, e1;
+      get_indx(c, bx, by, &s0, &e0, &s1, &e1);
+      c->blk[b] = int4{s0, e0, s1, e1};
+      for (int i = s0; i <= e0; ++i) c->lat_block[i - 1] = bx - 1;
+      for (int i = s1; i <= e1; ++i) c->lon_block[i - 1] = by - 1;
+      neighbour_blocks(c, bx, by, c->nb_blk);
+      c->nb_off[b + 1] = (int)c->nb_blk.size();
+    }
+  dfree(c->d_glat); dfree(c->d_glon); dfree(c->d_ca); dfree(c->d_cb); dfree(c->d_blk);
+  dfree(c->d_lat_block); dfree(c->d_lon_block); dfree(c->d_nb_off); dfree(c->d_nb_blk);
+  int r = LG_OK;
+  r |= dalloc(&c->d_glat, g.num_lat + 1);
+  r |= dalloc(&c->d_glon, g.num_lon + 1);
+  r |= dalloc(&c->d_ca, g.nz + 1);
+  r |= dalloc(&c->d_cb, g.nz + 1);
+  r |= dalloc(&c->d_blk, nb);
+  r |= dalloc(&c->d_lat_block, g.num_lat);
+  r |= dalloc(&c->d_lon_block, g.num_lon);
+  r |= dalloc(&c->d_nb_off, nb + 1);
+  r |= dalloc(&c->d_nb_blk, c->nb_blk.size());
+  if (r != LG_OK) return LG_ERR_NOMEM;
+  std::vector<double> cb(g.nz + 1, 0.0);
+  if (coef_b) cb.assign(coef_b, coef_b + g.nz + 1);
+  CK(cudaMemcpy(c->d_glat, c->glat.data(), sizeof(float) * (g.num_lat + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_glon, c->glon.data(), sizeof(float) * (g.num_lon + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_ca, coef_a, sizeof(double) * (g.nz + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_cb, cb.data(), sizeof(double) * (g.nz + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_blk, c->blk.data(), sizeof(int4) * nb, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_lat_block, c->lat_block.data(), sizeof(int) * g.num_lat, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_lon_block, c->lon_block.data(), sizeof(int) * g.num_lon, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_nb_off, c->nb_off.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice));
+  if (!c->nb_blk.empty())
+    CK(cudaMemcpy(c->d_nb_blk, c->nb_blk.data(), sizeof(int) * c->nb_blk.size(), cudaMemcpyHostToDevice));
+  Geometry& geo = c->geo;
+  geo.p0 = p0;
+  geo.ptop = ptop;
+  geo.glat = c->d_glat;
+  geo.glon = c->d_glon;
+  geo.ca = c->d_ca;
+  geo.cb = c->d_cb;
+  geo.blk = c->d_blk;
+  geo.lat_block = c->d_lat_block;
+  geo.lon_block = c->d_lon_block;
+  geo.nb_off = c->d_nb_off;
+  geo.nb_blk = c->d_nb_blk;
+  c->have_grid = true;
+  return LG_OK;
+}
+
+int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
+  if (!c || !o) return LG_ERR_ARG;
+  if (!c->have_grid) return LG_ERR_STATE;
+  if (o->n_types < 1 || o->n_types > LG_MAX_OBS_TYPES || o->n_obs < 0) return LG_ERR_ARG;
+  if (o->n_obs > 0 && (!o->type || !o->lat || !o->lon || !o->ph || !o->yo || !o->rinv))
+    return LG_ERR_ARG;
+  const lg_config& g = c->cfg;
+  lg::TypeTable tt{};
+  tt.n_types = o->n_types;
+  for (int t = 0; t < o->n_types; ++t) {
+    const lg_obs_type& ty = o->types[t];
+    if (ty.nz < 1 || ty.nz > 64 || ty.nvar < 1 || ty.nvar > LG_MAX_OBS_VARS) return LG_ERR_ARG;
+    tt.nz[t] = ty.nz;
+    tt.nvar[t] = ty.nvar;
+    for (int v = 0; v < ty.nvar; ++v) {
+      if (ty.var[v] < 0 || ty.var[v] >= g.n_var) return LG_ERR_VARNAME;
+      tt.var[t][v] = ty.var[v];
+    }
+  }
+  free_obs(c);
+  const int n = o->n_obs, T = o->n_types;
+  std::vector<int64_t> ph_off(n + 1, 0), val_off(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    const int t = o->type[i];
+    if (t < 0 || t >= T) return LG_ERR_ARG;
+    ph_off[i + 1] = ph_off[i] + tt.nz[t];
+    val_off[i + 1] = val_off[i] + (int64_t)tt.nz[t] * tt.nvar[t];
+  }
+  // block box queries: an observation belongs to every block whose inclusive
+  // %.5f bounds contain it (1, 2 or 4 blocks)
+  const int nb = g.global_nx * g.global_ny;
+  std::vector<double> lo_lat(g.global_nx), hi_lat(g.global_nx), lo_lon(g.global_ny), hi_lon(g.global_ny);
+  for (int bx = 1; bx <= g.global_nx; ++bx) {
+    const int4 b = c->blk[bx - 1];
+    lo_lat[bx - 1] = box_bound(GL(c, b.x));
+    hi_lat[bx - 1] = box_bound(GL(c, b.y + 1));
+  }
+  for (int by = 1; by <= g.global_ny; ++by) {
+    const int4 b = c->blk[(by - 1) * g.global_nx];
+    lo_lon[by - 1] = box_bound(GN(c, b.z));
+    hi_lon[by - 1] = box_bound(GN(c, b.w + 1));
+  }
+  std::vector<int> bt_cnt((size_t)nb * T + 1, 0);
+  std::vector<int> rows_of(n * 2), cols_of(n * 2);
+  std::vector<unsigned char> nrow(n), ncolb(n);
+  for (int i = 0; i < n; ++i) {
+    const double la = o->lat[i], lo = o->lon[i];
+    int nr = 0, nc = 0;
+    // blocks are contiguous in latitude: binary search for the first
+    int a = (int)(std::lower_bound(hi_lat.begin(), hi_lat.end(), la) - hi_lat.begin());
+    for (int bx = a; bx < g.global_nx && nr < 2; ++bx) {
+      if (la < lo_lat[bx]) break;
+      if (la <= hi_lat[bx]) rows_of[2 * i + nr++] = bx;
+    }
+    int bcol = (int)(std::lower_bound(hi_lon.begin(), hi_lon.end(), lo) - hi_lon.begin());
+    for (int by = bcol; by < g.global_ny && nc < 2; ++by) {
+      if (lo < lo_lon[by]) break;
+      if (lo <= hi_lon[by]) cols_of[2 * i + nc++] = by;
+    }
+    nrow[i] = (unsigned char)nr;
+    ncolb[i] = (unsigned char)nc;
+    for (int r = 0; r < nr; ++r)
+      for (int q = 0; q < nc; ++q)
+        bt_cnt[((size_t)cols_of[2 * i + q] * g.global_nx + rows_of[2 * i + r]) * T + o->type[i]]++;
+  }
+  std::vector<int> bt_off((size_t)nb * T + 1, 0);
+  for (size_t s = 0; s < (size_t)nb * T; ++s) bt_off[s + 1] = bt_off[s] + bt_cnt[s];
+  const int64_t ncopies = bt_off[(size_t)nb * T];
+  c->h_copy_obs.assign(ncopies, 0);
+  c->h_copy_block.assign(ncopies, 0);
+  {
+    std::vector<int> fill(bt_off.begin(), bt_off.end() - 1);
+    for (int i = 0; i < n; ++i)
+      for (int r = 0; r < nrow[i]; ++r)
+        for (int q = 0; q < ncolb[i]; ++q) {
+          const int b = cols_of[2 * i + q] * g.global_nx + rows_of[2 * i + r];
+          const int j = fill[(size_t)b * T + o->type[i]]++;
+          c->h_copy_obs[j] = i;
+          c->h_copy_block[j] = b;
+        }
+  }
+  c->h_copy_eoff.assign(ncopies + 1, 0);
+  int64_t ent = 0;
+  for (int64_t j = 0; j < ncopies; ++j) {
+    c->h_copy_eoff[j] = (int)ent;
+    const int t = o->type[c->h_copy_obs[j]];
+    ent += (int64_t)tt.nz[t] * tt.nvar[t];
+    if (ent > 0x7fffffff) return LG_ERR_SHAPE;
+  }
+  c->h_copy_eoff[ncopies] = (int)ent;
+  // upload
+  lg::ObsDev& d = c->obs;
+  d.n_obs = n;
+  d.n_copies = ncopies;
+  d.n_entries = ent;
+  int r = LG_OK;
+  r |= upload(c, o->type, n, &d.otype);
+  r |= upload(c, o->lat, n, &d.olat);
+  r |= upload(c, o->lon, n, &d.olon);
+  r |= upload(c, ph_off.data(), n + 1, &d.ph_off);
+  r |= upload(c, val_off.data(), n + 1, &d.val_off);
+  r |= upload(c, o->ph, (size_t)ph_off[n], &d.oph);
+  r |= upload(c, o->yo, (size_t)val_off[n], &d.oyo);
+  r |= upload(c, o->rinv, (size_t)val_off[n], &d.orinv);
+  r |= upload(c, c->h_copy_obs.data(), ncopies, &d.copy_obs);
+  r |= upload(c, c->h_copy_block.data(), ncopies, &d.copy_block);
+  r |= upload(c, c->h_copy_eoff.data(), ncopies + 1, &d.copy_eoff);
+  r |= upload(c, bt_off.data(), (size_t)nb * T + 1, &d.bt_off);
+  double *dcx, *dsx, *dyr;
+  float *fcx, *fsx, *fyr;
+  r |= scratch(c, n, &dcx);
+  r |= scratch(c, n, &dsx);
+  r |= scratch(c, n, &dyr);
+  r |= scratch(c, n, &fcx);
+  r |= scratch(c, n, &fsx);
+  r |= scratch(c, n, &fyr);
+  if (r != LG_OK) {
+    free_obs(c);
+    return r < 0 ? r : LG_ERR_NOMEM;
+  }
+  d.dcx = dcx; d.dsx = dsx; d.dyr = dyr; d.fcx = fcx; d.fsx = fsx; d.fyr = fyr;
+  lg::launch_obs_trig(d, dcx, dsx, dyr, fcx, fsx, fyr, c->own_stream);
+  c->types = tt;
+  c->geo.n_types = T;
+  lg::set_type_table(tt, c->own_stream);
+  CK(cudaStreamSynchronize(c->own_stream));
+  if (ensure_hx(c, (size_t)ent) != LG_OK) {
+    free_obs(c);
+    return LG_ERR_NOMEM;
+  }
+  c->have_obs = true;
+  return LG_OK;
+}
+
+int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* xa,
+                  double* axa, void* stream_v) {
+  (void)ntimes;
+  if (!c || !xb || !axb || !xa || !axa) return LG_ERR_ARG;
+  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
+  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+  const lg_config& g = c->cfg;
+  const Geometry& geo = c->geo;
+  const int ncol = g.num_lat * g.num_lon;
+  const int k = g.ens;
+  lg_stats& S = c->stats;
+  memset(&S, 0, sizeof S);
+  // list bookkeeping buffers
+  if (!c->lists.cnt) {
+    int r = LG_OK;
+    r |= dalloc(&c->lists.cnt, ncol + 1);
+    r |= dalloc(&c->lists.off, ncol + 1);
+    r |= dalloc(&c->lists.capped, ncol);
+    c->scan_tmp_bytes = lg::scan_tmp_bytes(ncol);
+    r |= dalloc((char**)&c->d_scan_tmp, c->scan_tmp_bytes);
+    if (r != LG_OK) return LG_ERR_NOMEM;
+  }
+  CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * 4, st));
+  CK(cudaMemsetAsync(c->d_band, 0, sizeof(unsigned long long), st));
+  CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
+  CK(cudaEventRecord(c->ev[0], st));
+  // H(x)
+  lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, st);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(c->ev[1], st));
+  // selection: count, scan, fill
+  lg::launch_search(geo, c->obs, c->lists, 0, c->d_band, st);
+  lg::launch_scan_counts(c->lists.cnt, c->lists.off, ncol, c->d_scan_tmp, c->scan_tmp_bytes, st);
+  int64_t total = 0;
+  CK(cudaMemcpyAsync(&total, c->lists.off + ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if ((size_t)total > c->list_cap || !c->lists.ent) {
+    dfree(c->lists.ent);
+    dfree(c->lists.rloc);
+    const size_t cap = (size_t)total + (size_t)total / 8 + 1024;
+    if (dalloc(&c->lists.ent, cap) != LG_OK || dalloc(&c->lists.rloc, cap) != LG_OK) {
+      c->list_cap = 0;
+      return LG_ERR_NOMEM;
+    }
+    c->list_cap = cap;
+  }
+  c->list_total = total;
+  lg::launch_search(geo, c->obs, c->lists, 1, nullptr, st);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(c->ev[2], st));
+  // solves, in column chunks bounded by the Gram workspace
+  const int levels = g.vert_dist > 0.0 ? g.nz : 1;
+  const size_t per_col = (size_t)levels * k * k;
+  int chunk = (int)std::min<size_t>((size_t)ncol, std::max<size_t>(1, ((size_t)256 << 20) / per_col));
+  if ((size_t)chunk * levels > c->solve_cap) {
+    dfree(c->d_C);
+    dfree(c->d_t);
+    const size_t cap = (size_t)chunk * levels;
+    if (dalloc(&c->d_C, cap * k * k) != LG_OK || dalloc(&c->d_t, cap * k) != LG_OK) {
+      c->solve_cap = 0;
+      return LG_ERR_NOMEM;
+    }
+    c->solve_cap = cap;
+  }
+  for (int c0 = 0; c0 < ncol; c0 += chunk) {
+    lg::SolveBatch b{};
+    b.mode = 0;
+    b.first_col = c0;
+    b.ncols = std::min(chunk, ncol - c0);
+    b.levels = levels;
+    b.nsolves = b.ncols * levels;
+    lg::launch_gram64(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, st);
+    lg::launch_eig_apply(geo, b, c->d_C, c->d_t, xb, axb, xa, axa, nullptr, nullptr,
+                         c->d_status + 1, st);
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(c->ev[3], st));
+  int status[4];
+  unsigned long long band = 0;
+  CK(cudaMemcpyAsync(status, c->d_status, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&band, c->d_band, sizeof(band), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  float ms;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); S.ms_hx = ms;
+  cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); S.ms_search = ms;
+  cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); S.ms_solve = ms;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]); S.ms_total = ms;
+  S.n_columns = ncol;
+  S.n_solves = (int64_t)ncol * levels;
+  S.n_copies = c->obs.n_copies;
+  S.n_entries = c->obs.n_entries;
+  S.nobsl_total = total;
+  S.n_band = (int64_t)band;
+  S.n_eig_fail = status[1];
+  if (status[0] != 0) return status[0];
+  return LG_OK;
+}
+
+int lg_run(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* xa, double* axa) {
+  if (!c || !xb || !axb || !xa || !axa) return LG_ERR_ARG;
+  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
+  const lg_config& g = c->cfg;
+  const size_t nlat_e = g.num_lat + 2 * g.halo, nlon_e = g.num_lon + 2 * g.halo;
+  const size_t cols = nlat_e * nlon_e;
+  const size_t n = c->geo.n, k = g.ens;
+  if (c->state_elems < cols * n * k) {
+    dfree(c->d_xb); dfree(c->d_axb); dfree(c->d_xa); dfree(c->d_axa);
+    int r = LG_OK;
+    r |= dalloc(&c->d_xb, cols * n * k);
+    r |= dalloc(&c->d_xa, cols * n * k);
+    r |= dalloc(&c->d_axb, cols * n);
+    r |= dalloc(&c->d_axa, cols * n);
+    if (r != LG_OK) { c->state_elems = 0; return LG_ERR_NOMEM; }
+    c->state_elems = cols * n * k;
+  }
+  cudaStream_t st = c->own_stream;
+  CK(cudaMemcpyAsync(c->d_xb, xb, sizeof(double) * cols * n * k, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_axb, axb, sizeof(double) * cols * n, cudaMemcpyHostToDevice, st));
+  int r = lg_run_device(c, ntimes, c->d_xb, c->d_axb, c->d_xa, c->d_axa, st);
+  if (r != LG_OK) return r;
+  // interior columns only: for each longitude the interior latitudes are contiguous
+  const size_t h = g.halo;
+  const size_t pitch_x = nlat_e * n * k * sizeof(double), pitch_a = nlat_e * n * sizeof(double);
+  const size_t off_x = (h + h * nlat_e) * n * k, off_a = (h + h * nlat_e) * n;
+  CK(cudaMemcpy2DAsync(xa + off_x, pitch_x, c->d_xa + off_x, pitch_x,
+                       (size_t)g.num_lat * n * k * sizeof(double), g.num_lon,
+                       cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpy2DAsync(axa + off_a, pitch_a, c->d_axa + off_a, pitch_a,
+                       (size_t)g.num_lat * n * sizeof(double), g.num_lon,
+                       cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return LG_OK;
+}
+
+int lg_get_stats(const lg_ctx* c, lg_stats* st) {
+  if (!c || !st) return LG_ERR_ARG;
+  *st = c->stats;
+  return LG_OK;
+}
+
+int lg_get_lists(const lg_ctx* c, int* counts, int* entries, double* rloc, int64_t* total) {
+  if (!c || !total) return LG_ERR_ARG;
+  if (!c->lists.off) return LG_ERR_STATE;
+  *total = c->list_total;
+  const int ncol = c->cfg.num_lat * c->cfg.num_lon;
+  if (counts) CK(cudaMemcpy(counts, c->lists.cnt, sizeof(int) * ncol, cudaMemcpyDeviceToHost));
+  if (entries && c->list_total)
+    CK(cudaMemcpy(entries, c->lists.ent, sizeof(int) * c->list_total, cudaMemcpyDeviceToHost));
+  if (rloc && c->list_total)
+    CK(cudaMemcpy(rloc, c->lists.rloc, sizeof(double) * c->list_total, cudaMemcpyDeviceToHost));
+  return LG_OK;
+}
+
+int lg_copy_layout(const lg_ctx* c, int* copy_obs, int* copy_block, int64_t* copy_entry_off,
+                   int64_t* n_copies) {
+  if (!c || !n_copies) return LG_ERR_ARG;
+  if (!c->have_obs) return LG_ERR_STATE;
+  const int64_t n = (int64_t)c->h_copy_obs.size();
+  *n_copies = n;
+  if (copy_obs) memcpy(copy_obs, c->h_copy_obs.data(), sizeof(int) * n);
+  if (copy_block) memcpy(copy_block, c->h_copy_block.data(), sizeof(int) * n);
+  if (copy_entry_off)
+    for (int64_t j = 0; j <= n; ++j) copy_entry_off[j] = c->h_copy_eoff[j];
+  return LG_OK;
+}
+
+int lg_get_hx(const lg_ctx* c, double* yb, double* dis) {
+  if (!c) return LG_ERR_ARG;
+  if (!c->have_obs) return LG_ERR_STATE;
+  const size_t ne = (size_t)c->obs.n_entries;
+  if (yb) CK(cudaMemcpy(yb, c->hx.yb, sizeof(double) * ne * c->cfg.ens, cudaMemcpyDeviceToHost));
+  if (dis) CK(cudaMemcpy(dis, c->hx.dis, sizeof(double) * ne, cudaMemcpyDeviceToHost));
+  return LG_OK;
+}
+
+void lg_destroy(lg_ctx* c) {
+  if (!c) return;
+  free_obs(c);
+  dfree(c->d_glat); dfree(c->d_glon); dfree(c->d_ca); dfree(c->d_cb); dfree(c->d_blk);
+  dfree(c->d_lat_block); dfree(c->d_lon_block); dfree(c->d_nb_off); dfree(c->d_nb_blk);
+  dfree(c->hx.yb); dfree(c->hx.yb32); dfree(c->hx.dis); dfree(c->hx.lnp); dfree(c->hx.rdiag);
+  dfree(c->lists.cnt); dfree(c->lists.off); dfree(c->lists.ent); dfree(c->lists.rloc);
+  dfree(c->lists.capped);
+  if (c->d_scan_tmp) cudaFree(c->d_scan_tmp);
+  dfree(c->d_C); dfree(c->d_t); dfree(c->d_status); dfree(c->d_band);
+  dfree(c->d_xb); dfree(c->d_axb); dfree(c->d_xa); dfree(c->d_axa);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+}
+
+int lg_core_batch(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
+                  const double* d_hxens, const float* d_rdiaginv, const double* d_dep,
+                  const double* d_rloc, double inflation, int precision, double* d_trans,
+                  double* d_wbar, void* stream_v) {
+  if (ens < 2 || ens > 128 || nbatch < 0 || inflation <= 0.0) return LG_ERR_ARG;
+  if (precision != LG_PREC_FP64 && precision != LG_PREC_MIXED) return LG_ERR_ARG;
+  if (nbatch == 0) return LG_OK;
+  if (!d_nobsl || !d_off || !d_trans || !d_wbar) return LG_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream_v;
+  Geometry geo{};
+  geo.ens = ens;
+  geo.inflation = inflation;
+  geo.vert_dist = -1.0;
+  lg::SolveBatch b{};
+  b.mode = 1;
+  b.nsolves = nbatch;
+  b.levels = 1;
+  b.b_nobsl = d_nobsl;
+  b.b_off = d_off;
+  b.b_hx = d_hxens;
+  b.b_rdiag = d_rdiaginv;
+  b.b_dep = d_dep;
+  b.b_rloc = d_rloc;
+  double *C = nullptr, *t = nullptr;
+  int* fail = nullptr;
+  if (dalloc(&C, (size_t)nbatch * ens * ens) != LG_OK || dalloc(&t, (size_t)nbatch * ens) != LG_OK ||
+      dalloc(&fail, 1) != LG_OK) {
+    dfree(C); dfree(t); dfree(fail);
+    return LG_ERR_NOMEM;
+  }
+  int result = LG_OK;
+  cudaMemsetAsync(fail, 0, sizeof(int), st);
+  lg::HxDev hx{};
+  lg::ListDev l{};
+  lg::launch_gram64(geo, hx, l, b, nullptr, C, t, st);
+  lg::launch_eig_apply(geo, b, C, t, nullptr, nullptr, nullptr, nullptr, d_trans, d_wbar, fail, st);
+  int h_fail = 0;
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(&h_fail, fail, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    result = LG_ERR_CUDA;
+  else if (h_fail)
+    result = LG_ERR_EIG;
+  dfree(C); dfree(t); dfree(fail);
+  return result;
+}
+
+int lg_letkf_core(int nanals, int nobsl, const double* hxens, const float* rdiaginv,
+                  const double* dep, const double* rloc, double* trans, double* overline_w,
+                  double inflation_factor) {
+  if (nanals < 2 || nanals > 128 || nobsl < 0 || !trans || !overline_w) return LG_ERR_ARG;
+  if (nobsl > 0 && (!hxens || !rdiaginv || !dep || !rloc)) return LG_ERR_ARG;
+  double *dh = nullptr, *dd = nullptr, *dr = nullptr, *dt = nullptr, *dw = nullptr;
+  float* df = nullptr;
+  int* dn = nullptr;
+  int64_t* doff = nullptr;
+  const size_t p = (size_t)nobsl, k = (size_t)nanals;
+  int r = LG_OK;
+  r |= dalloc(&dh, p * k);
+  r |= dalloc(&df, p);
+  r |= dalloc(&dd, p);
+  r |= dalloc(&dr, p);
+  r |= dalloc(&dt, k * k);
+  r |= dalloc(&dw, k);
+  r |= dalloc(&dn, 1);
+  r |= dalloc(&doff, 1);
+  if (r == LG_OK) {
+    const int64_t zero = 0;
+    if (p) {
+      cudaMemcpy(dh, hxens, sizeof(double) * p * k, cudaMemcpyHostToDevice);
+      cudaMemcpy(df, rdiaginv, sizeof(float) * p, cudaMemcpyHostToDevice);
+      cudaMemcpy(dd, dep, sizeof(double) * p, cudaMemcpyHostToDevice);
+      cudaMemcpy(dr, rloc, sizeof(double) * p, cudaMemcpyHostToDevice);
+    }
+    cudaMemcpy(dn, &nobsl, sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(doff, &zero, sizeof(int64_t), cudaMemcpyHostToDevice);
+    r = lg_core_batch(nanals, 1, dn, doff, dh, df, dd, dr, inflation_factor, LG_PREC_FP64, dt, dw,
+                      nullptr);
+    if (r == LG_OK || r == LG_ERR_EIG) {
+      if (cudaMemcpy(trans, dt, sizeof(double) * k * k, cudaMemcpyDeviceToHost) != cudaSuccess ||
+          cudaMemcpy(overline_w, dw, sizeof(double) * k, cudaMemcpyDeviceToHost) != cudaSuccess)
+        r = LG_ERR_CUDA;
+    }
+  } else {
+    r = LG_ERR_NOMEM;
+  }
+  dfree(dh); dfree(df); dfree(dd); dfree(dr); dfree(dt); dfree(dw); dfree(dn); dfree(doff);
+  return r;
+}
+
+void letkf_core_(const int* nanals, const int* nobsl, const double* hxens, const float* rdiaginv,
+                 const double* dep, const double* rloc, double* trans, double* overline_w,
+                 const double* inflation_factor, const int* pflag) {
+  (void)pflag;
+  const int r = lg_letkf_core(*nanals, *nobsl, hxens, rdiaginv, dep, rloc, trans, overline_w,
+                              *inflation_factor);
+  if (r != LG_OK && r != LG_ERR_EIG) fprintf(stderr, "letkf_core_: %s\n", lg_status_string(r));
+}
+
+}  // extern "C"

@@ -1,0 +1,232 @@
+// lg_hx.cu -- observation operator H(x) for every member (FP64).
+//
+// One warp per block-observation copy.  Restates, per copy:
+//   find_obs_grid           x86/DA/LETKF/src/letkf_obs.F90:192-248
+//   ps2ph_3d_interp         x86/DA/LETKF/src/obs_make.F90:345-381
+//   obs_interpolation_3d_2  x86/DA/LETKF/src/obs_make.F90:233-342
+//   member-mean removal     x86/DA/LETKF/src/letkf_obs.F90:156-183
+// with the reference's operation order and no contraction (this file is built
+// with -fmad=false).  Lanes own members e = lane, lane+32, ...; the member mean
+// is summed sequentially in member order, as the Fortran loop does.
+#include "lg_device.cuh"
+#include "lg_internal.h"
+
+namespace lg {
+
+__constant__ TypeTable c_types;
+
+void set_type_table(const TypeTable& t, cudaStream_t stream) {
+  cudaMemcpyToSymbolAsync(c_types, &t, sizeof(TypeTable), 0, cudaMemcpyHostToDevice, stream);
+}
+
+__global__ void obs_trig_kernel(int n, const double* lat, const double* lon, double* dcx,
+                                double* dsx, double* dyr, float* fcx, float* fsx, float* fyr) {
+  int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  double xr = deg2rad_r8(lat[o]);
+  dcx[o] = cos(xr);
+  dsx[o] = sin(xr);
+  dyr[o] = deg2rad_r8(lon[o]);
+  const float pf = 3.14159274101257324f;
+  float xf = (float)lat[o] / 180.0f * pf;
+  fcx[o] = cosf(xf);
+  fsx[o] = sinf(xf);
+  fyr[o] = (float)lon[o] / 180.0f * pf;
+}
+
+void launch_obs_trig(const ObsDev& o, double* dcx, double* dsx, double* dyr, float* fcx,
+                     float* fsx, float* fyr, cudaStream_t stream) {
+  if (o.n_obs == 0) return;
+  obs_trig_kernel<<<(o.n_obs + 255) / 256, 256, 0, stream>>>(o.n_obs, o.olat, o.olon, dcx, dsx,
+                                                               dyr, fcx, fsx, fyr);
+}
+
+// da_vert_coord_calc_ph_lev (x86/DA/utils/vert_coord_mod.F90:547-563), k 1-based
+__device__ inline double calc_ph_lev(const Geometry& g, int k, double phs) {
+  if (g.vcoord == LG_VCOORD_SIGMA)
+    return __dadd_rn(__dmul_rn(g.ca[k - 1], __dsub_rn(phs, g.ptop)), g.ptop);
+  double t1 = __dmul_rn(g.ca[k - 1], __dsub_rn(g.p0, g.ptop));
+  double t2 = __dmul_rn(g.cb[k - 1], __dsub_rn(phs, g.ptop));
+  return __dadd_rn(__dadd_rn(t1, t2), g.ptop);
+}
+
+// half-level pressure ph(j) = 0.5*(ph_lev(j)+ph_lev(j+1)), j = 1..nz, ph(nz+1) = ph(nz)
+__device__ inline double half_ph(const Geometry& g, int j, double ps) {
+  if (j > g.nz) j = g.nz;
+  return __dmul_rn(0.5, __dadd_rn(calc_ph_lev(g, j, ps), calc_ph_lev(g, j + 1, ps)));
+}
+
+// bilinear value (r1*t2 + r2*(1-t2)) of row r at the 2x2 stencil for member e
+__device__ inline double bilin(const double* xb, const double* axb, int k, int n, int e, int r,
+                               size_t c11, size_t c21, size_t c12, size_t c22, double t1,
+                               double t2) {
+  const double u1 = __dsub_rn(1.0, t1), u2 = __dsub_rn(1.0, t2);
+  double a11 = __dadd_rn(xb[e + (size_t)k * (r + (size_t)n * c11)], axb[r + (size_t)n * c11]);
+  double a21 = __dadd_rn(xb[e + (size_t)k * (r + (size_t)n * c21)], axb[r + (size_t)n * c21]);
+  double a12 = __dadd_rn(xb[e + (size_t)k * (r + (size_t)n * c12)], axb[r + (size_t)n * c12]);
+  double a22 = __dadd_rn(xb[e + (size_t)k * (r + (size_t)n * c22)], axb[r + (size_t)n * c22]);
+  double r1 = __dadd_rn(__dmul_rn(a11, t1), __dmul_rn(a21, u1));
+  double r2 = __dadd_rn(__dmul_rn(a12, t1), __dmul_rn(a22, u1));
+  return __dadd_rn(__dmul_rn(r1, t2), __dmul_rn(r2, u2));
+}
+
+constexpr int kMaxMemberSlots = 4;  // ens <= 128
+
+__global__ void __launch_bounds__(128) hx_kernel(Geometry g, ObsDev ob, const double* xb,
+                                                 const double* axb, HxDev hx, int* err) {
+  const int64_t j = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x / 32);
+  if (j >= ob.n_copies) return;
+  const unsigned lane = threadIdx.x & 31u;
+  const int k = g.ens, n = g.n;
+  const int o = ob.copy_obs[j];
+  const int4 bk = g.blk[ob.copy_block[j]];
+  const int s_lat = bk.x, e_lat = bk.y, s_lon = bk.z, e_lon = bk.w;
+  const int nxl = e_lat - s_lat + 1, nyl = e_lon - s_lon + 1;
+  const double lat = ob.olat[o], lon = ob.olon[o];
+  // find_obs_grid: first local index with grid >= obs coordinate
+  int tx = 0, ty = 0;
+  for (int base = 1; base <= nxl + 1 && tx == 0; base += 32) {
+    int i = base + (int)lane;
+    bool hit = (i <= nxl + 1) && ((double)g.glat[s_lat + i - 2] >= lat);
+    unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (m) tx = base + __ffs(m) - 1;
+  }
+  for (int base = 1; base <= nyl + 1 && ty == 0; base += 32) {
+    int i = base + (int)lane;
+    bool hit = (i <= nyl + 1) && ((double)g.glon[s_lon + i - 2] >= lon);
+    unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (m) ty = base + __ffs(m) - 1;
+  }
+  const int ti = c_types.nz[0] >= 0 ? ob.otype[o] : 0;
+  const int onz = c_types.nz[ti], onv = c_types.nvar[ti];
+  const int64_t ebase = ob.copy_eoff[j];
+  if (tx == 0 || ty == 0) {
+    if (lane == 0) atomicExch(err, LG_ERR_OBS_OUTSIDE);
+    return;
+  }
+  double ax = 0.0, ay = 0.0;
+  if (tx > 1) {
+    float gt = g.glat[s_lat + tx - 2], gp = g.glat[s_lat + tx - 3];
+    double dlat = (double)__fsub_rn(gt, gp);  // REAL(4) subtraction
+    ax = __ddiv_rn(__dadd_rn(__dsub_rn(dlat, lat), (double)gp), dlat);
+  }
+  if (ty > 1) {
+    float gt = g.glon[s_lon + ty - 2], gp = g.glon[s_lon + ty - 3];
+    double dlon = (double)__fsub_rn(gt, gp);
+    ay = __ddiv_rn(__dadd_rn(__dsub_rn(dlon, lon), (double)gp), dlon);
+  }
+  const int nlat_e = g.num_lat + 2 * g.halo;
+  auto colidx = [&](int glat, int glon) -> size_t {
+    return (size_t)(glat - 1 + g.halo) + (size_t)nlat_e * (size_t)(glon - 1 + g.halo);
+  };
+  const int la0 = s_lat + tx - 2, la1 = s_lat + tx - 1;
+  const int lo0 = s_lon + ty - 2, lo1 = s_lon + ty - 1;
+  const size_t c11 = colidx(la0, lo0), c21 = colidx(la1, lo0);
+  const size_t c12 = colidx(la0, lo1), c22 = colidx(la1, lo1);
+  const double t1 = ax, t2 = ay;
+  const double* oph = ob.oph + ob.ph_off[o];
+  const double* yo = ob.oyo + ob.val_off[o];
+  const double* ri = ob.orinv + ob.val_off[o];
+
+  double ps[kMaxMemberSlots];
+#pragma unroll
+  for (int q = 0; q < kMaxMemberSlots; ++q) {
+    const int e = (int)lane + 32 * q;
+    ps[q] = (e < k) ? bilin(xb, axb, k, n, e, g.ps_row, c11, c21, c12, c22, t1, t2) : 0.0;
+  }
+  // ph_pos for each obs level; the search index persists across levels
+  // (obs_make.F90:252-272).  Levels are processed in order; at most 64 per type.
+  int jj[kMaxMemberSlots];
+#pragma unroll
+  for (int q = 0; q < kMaxMemberSlots; ++q) jj[q] = 1;
+  for (int l = 0; l < onz; ++l) {
+    const double po = oph[l];
+    const double lnpo = log(po);
+    int pp[kMaxMemberSlots];
+#pragma unroll
+    for (int q = 0; q < kMaxMemberSlots; ++q) {
+      const int e = (int)lane + 32 * q;
+      if (e < k) {
+        while (jj[q] <= g.nz && po > half_ph(g, jj[q], ps[q])) jj[q]++;
+      }
+      pp[q] = jj[q] - 1;
+    }
+    for (int kv = 0; kv < onv; ++kv) {
+      const int vid = c_types.var[ti][kv];
+      const int vs = g.var_start[vid];
+      const int64_t ent = ebase + (int64_t)l * onv + kv;
+      double y[kMaxMemberSlots];
+#pragma unroll
+      for (int q = 0; q < kMaxMemberSlots; ++q) {
+        const int e = (int)lane + 32 * q;
+        y[q] = 0.0;
+        if (e >= k) continue;
+        if (g.var_lev[vid] > 1) {
+          const int p = pp[q];
+          if (p >= 1 && p < g.nz) {
+            const int tl = vs + p - 1;
+            const double php1 = half_ph(g, p + 1, ps[q]), php = half_ph(g, p, ps[q]);
+            const double lp1 = log(php1);
+            const double t3 = __ddiv_rn(__dsub_rn(lp1, lnpo), __dsub_rn(lp1, log(php)));
+            const double r1 = bilin(xb, axb, k, n, e, tl, c11, c21, c12, c22, t1, t2);
+            const double r3 = bilin(xb, axb, k, n, e, tl + 1, c11, c21, c12, c22, t1, t2);
+            y[q] = __dadd_rn(__dmul_rn(r1, t3), __dmul_rn(r3, __dsub_rn(1.0, t3)));
+          } else {
+            const int tl = (p == 0) ? vs : vs + g.nz - 1;
+            y[q] = bilin(xb, axb, k, n, e, tl, c11, c21, c12, c22, t1, t2);
+          }
+        } else {
+          y[q] = bilin(xb, axb, k, n, e, vs, c11, c21, c12, c22, t1, t2);
+        }
+      }
+      // sequential member sum in member order (letkf_obs.F90:160-164)
+      double sum_y = 0.0;
+#pragma unroll
+      for (int q = 0; q < kMaxMemberSlots; ++q) {
+        if (32 * q >= k) break;
+        for (int src = 0; src < 32; ++src) {
+          double v = __shfl_sync(0xffffffffu, y[q], src);
+          if (32 * q + src < k) sum_y = __dadd_rn(sum_y, v);
+        }
+      }
+      sum_y = __ddiv_rn(sum_y, (double)k);
+#pragma unroll
+      for (int q = 0; q < kMaxMemberSlots; ++q) {
+        const int e = (int)lane + 32 * q;
+        if (e < k) {
+          const double d = __dsub_rn(y[q], sum_y);
+          hx.yb[(size_t)ent * k + e] = d;
+          if (hx.yb32) hx.yb32[(size_t)ent * k + e] = (float)d;
+        }
+      }
+      if (lane == 0) {
+        hx.dis[ent] = __dsub_rn(yo[l * onv + kv], sum_y);
+        hx.lnp[ent] = lnpo;  // letkf_yb.F90:211, with the observation's own ph
+        hx.rdiag[ent] = (float)ri[l * onv + kv];
+      }
+    }
+  }
+}
+
+void launch_hx(const Geometry& g, const ObsDev& o, const double* xb, const double* axb,
+               HxDev hx, int* err, cudaStream_t stream) {
+  if (o.n_copies == 0) return;
+  const int warps = 4;
+  const int64_t blocks = (o.n_copies + warps - 1) / warps;
+  hx_kernel<<<(unsigned)blocks, 32 * warps, 0, stream>>>(g, o, xb, axb, hx, err);
+}
+
+__global__ void nan_check_kernel(const double* x, size_t n, int* err) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  bool bad = false;
+  for (; i < n; i += stride) bad |= (x[i] != x[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(err, LG_ERR_NAN);
+}
+
+void launch_nan_check(const double* x, size_t n, int* err, cudaStream_t stream) {
+  if (n == 0) return;
+  nan_check_kernel<<<152 * 8, 256, 0, stream>>>(x, n, err);
+}
+
+}  // namespace lg

@@ -1,0 +1,120 @@
+// lg_internal.h -- context layout and kernel entry points of the LETKF library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/letkf_gpu.h"
+
+namespace lg {
+
+// Observation-type tables, per analysis (constant memory, set by lg_set_obs).
+struct TypeTable {
+  int n_types;
+  int nz[LG_MAX_OBS_TYPES];
+  int nvar[LG_MAX_OBS_TYPES];
+  int var[LG_MAX_OBS_TYPES][LG_MAX_OBS_VARS];
+};
+
+// Geometry and model constants visible to all kernels.
+struct Geometry {
+  int ens, num_lat, num_lon, nz, halo, n, n_var, ps_row;  // ps_row 0-based
+  int var_start[LG_MAX_VARS];                             // 0-based first row
+  int var_lev[LG_MAX_VARS];
+  int vcoord;
+  double p0, ptop;
+  double local_dist, vert_dist, inflation, obs_polar;
+  int gc_filter, gc_filter_vertical, max_obs;
+  int global_nx, global_ny, nblocks, n_types;
+  // device arrays
+  const float* glat;     // num_lat+1
+  const float* glon;     // num_lon+1
+  const double* ca;      // nz+1
+  const double* cb;      // nz+1
+  const int4* blk;       // (s_lat, e_lat, s_lon, e_lon), 1-based, per block
+  const int* lat_block;  // num_lat: 0-based block row of each latitude
+  const int* lon_block;  // num_lon: 0-based block column of each longitude
+  const int* nb_off;     // nblocks+1
+  const int* nb_blk;     // neighbour blocks in traversal order
+};
+
+// Observations and their block copies on the device.
+struct ObsDev {
+  int n_obs;
+  int64_t n_copies, n_entries;
+  const int* otype;
+  const double* olat;
+  const double* olon;
+  const int64_t* ph_off;
+  const int64_t* val_off;
+  const double* oph;
+  const double* oyo;
+  const double* orinv;
+  // per observation trig terms for the distance test
+  const double* dcx;  // cos(lat/180*pi)
+  const double* dsx;  // sin(lat/180*pi)
+  const double* dyr;  // lon/180*pi
+  const float* fcx;
+  const float* fsx;
+  const float* fyr;
+  // copies
+  const int* copy_obs;
+  const int* copy_block;
+  const int* copy_eoff;  // n_copies+1 entry offsets
+  const int* bt_off;     // nblocks*n_types+1: copies of (block, type)
+};
+
+// H(x) results per copy entry.
+struct HxDev {
+  double* yb;     // n_entries * ens
+  float* yb32;    // n_entries * ens (mixed path operand)
+  double* dis;    // n_entries
+  double* lnp;    // n_entries, log(ph)
+  float* rdiag;   // n_entries, REAL(4) R^-1
+};
+
+// Per-column neighbour lists.
+struct ListDev {
+  int* cnt;          // columns
+  int64_t* off;      // columns+1
+  int* ent;          // total entries
+  double* rloc;      // total entries
+  int* capped;       // columns (1 if truncated at max_obs)
+};
+
+// A batch of LETKF solves: which list entries feed it and where results go.
+struct SolveBatch {
+  int mode;          // 0 = analysis columns, 1 = explicit core batch
+  int first_col;     // mode 0: first column of the chunk
+  int ncols;         // mode 0: columns in the chunk
+  int levels;        // solves per column (nz for the vertical path, else 1)
+  int nsolves;
+  // mode 1 inputs
+  const int* b_nobsl;
+  const int64_t* b_off;
+  const double* b_hx;
+  const float* b_rdiag;
+  const double* b_dep;
+  const double* b_rloc;
+};
+
+// kernels (host launchers), all asynchronous on `stream`
+void launch_obs_trig(const ObsDev& o, double* dcx, double* dsx, double* dyr, float* fcx,
+                     float* fsx, float* fyr, cudaStream_t stream);
+void set_type_table(const TypeTable& t, cudaStream_t stream);
+void launch_hx(const Geometry& g, const ObsDev& o, const double* xb, const double* axb,
+               HxDev hx, int* err, cudaStream_t stream);
+void launch_search(const Geometry& g, const ObsDev& o, ListDev l, int fill,
+                   unsigned long long* band, cudaStream_t stream);
+void launch_scan_counts(const int* cnt, int64_t* off, int n, void* tmp, size_t tmp_bytes,
+                        cudaStream_t stream);
+size_t scan_tmp_bytes(int n);
+void launch_gram64(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
+                   const double* axb, double* C, double* t, cudaStream_t stream);
+void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
+                      const double* xb, const double* axb, double* xa, double* axa,
+                      double* trans, double* wbar, int* eig_fail, cudaStream_t stream);
+void launch_nan_check(const double* x, size_t n, int* err, cudaStream_t stream);
+
+}  // namespace lg

@@ -1,0 +1,145 @@
+// lg_search.cu -- per-column local observation selection.
+//
+// Restates gen_yb_dis / gen_yb_dis_vertical's selection
+// (x86/DA/LETKF/src/letkf_yb.F90:75-146,176-234): for the column centre
+// (grid_lat(j), grid_lon(i)), visit the neighbour blocks of the column's block
+// in comm_info_init order, then observation types, then the block's
+// observations in index order; keep an observation when its Gaspari-Cohn (or
+// box) weight of ri = dist/local_dist is positive, i.e. ri <= 2, and append all
+// of its (level, variable) entries; stop at MAX_OBS entries.
+//
+// One warp per column, 32 candidates per step.  The decision is made in FP32
+// on the cosine of the angular distance when it is farther than 1e-5 from the
+// threshold cos(2L/a), and otherwise by the exact FP64 formula of
+// latlon_dist_r8 (pro_info.F90:149-161) evaluated without contraction, so the
+// kept set and its order equal the reference's.  Two passes: count, then fill
+// at the prefix-summed offsets.
+#include <cub/device/device_scan.cuh>
+
+#include "lg_device.cuh"
+#include "lg_internal.h"
+
+namespace lg {
+
+struct SearchArgs {
+  float vlo, vhi;  // FP32 cosine band around the threshold
+};
+
+__global__ void __launch_bounds__(256) search_kernel(Geometry g, ObsDev ob, ListDev l, int fill,
+                                                     SearchArgs sa, unsigned long long* band) {
+  const int col = blockIdx.x * (blockDim.x / 32) + (threadIdx.x / 32);
+  const int ncol = g.num_lat * g.num_lon;
+  if (col >= ncol) return;
+  const unsigned lane = threadIdx.x & 31u;
+  const int glat = col % g.num_lat + 1, glon = col / g.num_lat + 1;
+  const int b = g.lon_block[glon - 1] * g.global_nx + g.lat_block[glat - 1];
+  // column centre (letkf_yb.F90:23-24), REAL(4) grid promoted to REAL(8)
+  const double clat = (double)g.glat[glat - 1], clon = (double)g.glon[glon - 1];
+  const double ccx = cos(deg2rad_r8(clat)), csx = sin(deg2rad_r8(clat));
+  const double cyr = deg2rad_r8(clon);
+  const float pf = 3.14159274101257324f;
+  const float fcx = cosf((float)clat / 180.0f * pf), fsx = sinf((float)clat / 180.0f * pf);
+  const float fyr = (float)clon / 180.0f * pf;
+  const int T = g.n_types;
+  const int cap = g.max_obs > 0 ? g.max_obs : 0x7fffffff;
+  int64_t written = 0;  // entries appended so far (uncapped count)
+  const int64_t out0 = fill ? l.off[col] : 0;
+  unsigned long long nband = 0;
+  bool done = false;
+  for (int q = g.nb_off[b]; q < g.nb_off[b + 1] && !done; ++q) {
+    const int nbk = g.nb_blk[q];
+    for (int t = 0; t < T && !done; ++t) {
+      const int j0 = ob.bt_off[nbk * T + t], j1 = ob.bt_off[nbk * T + t + 1];
+      for (int jb = j0; jb < j1 && !done; jb += 32) {
+        const int j = jb + (int)lane;
+        bool keep = false;
+        double ri = 0.0;
+        int nent = 0;
+        if (j < j1) {
+          const int o = ob.copy_obs[j];
+          if (fabs(ob.olat[o]) <= g.obs_polar) {
+            const float v32 = ob.fcx[o] * fcx * cosf(ob.fyr[o] - fyr) + ob.fsx[o] * fsx;
+            const bool in_band = v32 <= sa.vhi && v32 >= sa.vlo;
+            // the keep decision is identical in both passes; the fill pass also
+            // evaluates ri exactly for every kept copy to obtain its weight
+            if (in_band || (fill && v32 > sa.vhi)) {
+              double dist = latlon_dist_pre(ob.dcx[o], ob.dsx[o], ob.dyr[o], ccx, csx, cyr);
+              ri = __ddiv_rn(__dmul_rn(dist, 1.0), g.local_dist);
+            }
+            if (in_band) {
+              keep = loc_fn(ri, g.gc_filter) > 0.0;
+              if (!fill && fabs(ri - 2.0) < 1e-12) nband++;
+            } else {
+              keep = v32 > sa.vhi;
+            }
+            if (keep) nent = ob.copy_eoff[j + 1] - ob.copy_eoff[j];
+          }
+        }
+        // inclusive warp prefix of entry counts
+        int incl = nent;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+          int v = __shfl_up_sync(0xffffffffu, incl, s);
+          if ((int)lane >= s) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (fill && keep) {
+          const double gc = (ri <= 2.0) ? loc_fn(ri, g.gc_filter) : 0.0;
+          const int64_t pos0 = written + incl - nent;
+          const int e0 = ob.copy_eoff[j];
+          for (int m = 0; m < nent; ++m) {
+            const int64_t pos = pos0 + m;
+            if (pos < cap) {
+              l.ent[out0 + pos] = e0 + m;
+              l.rloc[out0 + pos] = gc;
+            }
+          }
+        }
+        written += total;
+        if (written >= cap) done = true;
+      }
+    }
+  }
+  if (!fill && lane == 0) {
+    l.cnt[col] = (int)(written < cap ? written : cap);
+    if (l.capped) l.capped[col] = written >= cap;
+  }
+  if (!fill && band) {
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) nband += __shfl_down_sync(0xffffffffu, nband, s);
+    if (lane == 0 && nband) atomicAdd(band, nband);
+  }
+}
+
+void launch_search(const Geometry& g, const ObsDev& o, ListDev l, int fill,
+                   unsigned long long* band, cudaStream_t stream) {
+  const int ncol = g.num_lat * g.num_lon;
+  // cos(2L/a): ri <= 2  <=>  acos(v) <= 2L/a
+  const double th = 2.0 * g.local_dist / earth_r4();
+  SearchArgs sa;
+  if (th >= 3.14159) {
+    sa.vlo = -3.0f;
+    sa.vhi = -2.0f;  // everything within reach: every candidate is exact-checked (fill) or kept
+  } else {
+    const double v = cos(th);
+    sa.vlo = (float)(v - 1e-5);
+    sa.vhi = (float)(v + 1e-5);
+  }
+  const int warps = 8;
+  search_kernel<<<(ncol + warps - 1) / warps, 32 * warps, 0, stream>>>(g, o, l, fill, sa, band);
+}
+
+size_t scan_tmp_bytes(int n) {
+  size_t bytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, bytes, (const int*)nullptr, (int64_t*)nullptr, n + 1);
+  return bytes;
+}
+
+// off[i] = sum_{c<i} cnt[c] for i = 0..n (cnt[n] is read as the scan's
+// extra element, so the caller keeps cnt sized n+1 with cnt[n] = 0)
+void launch_scan_counts(const int* cnt, int64_t* off, int n, void* tmp, size_t tmp_bytes,
+                        cudaStream_t stream) {
+  cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, cnt, off, n + 1, stream);
+}
+
+}  // namespace lg

@@ -1,0 +1,217 @@
+/*
+ * letkf_gpu.h -- C ABI of the GB300 LETKF analysis step.
+ *
+ * Drop-in boundary for the LETKF analysis call of DIDA-THHPCA's DA component
+ * (x86/DA/LETKF).  Plain C, no C++ or CUDA types in any signature; every
+ * pointer is caller-owned; every entry point returns LG_OK (0) or a negative
+ * LG_ERR_* status and never aborts the process.
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   lg_create / lg_set_grid   <- letkf_init            x86/DA/LETKF/src/letkf_init.F90:2-98
+ *                                pro_info_init         x86/DA/utils/pro_info.F90:26-93
+ *                                da_vert_coord_init    x86/DA/utils/vert_coord_mod.F90:33-545
+ *   lg_set_obs                <- gen_obs_struct's Redis reads + comm_obs_data
+ *                                                     x86/DA/LETKF/src/letkf_obs.F90:16-98, 251-466
+ *                                                     x86/DA/LETKF/src/read_obs_mod.F90:73-449
+ *   lg_run / lg_run_device    <- letkf_run(ntimes, xb, axb, xa, axa)
+ *                                                     x86/DA/LETKF/src/letkf.F90:157-257
+ *   lg_core_batch             <- letkf_core (column-batched)
+ *                                                     x86/DA/LETKF/src/letkf_core.F90:14-233
+ *   letkf_core_               <- letkf_core, Fortran implicit-interface symbol
+ *                                (same ABI as sw/DA/LETKF/src/letkf_half/letkf_core_half_master.c:24-26)
+ *   lg_destroy                <- letkf_final           x86/DA/LETKF/src/letkf_final.F90:2-13
+ *
+ * Array conventions follow the reference exactly (Fortran column-major):
+ *   xb, xa  : double [ens][n][num_lat + 2*halo][num_lon + 2*halo] with ens fastest,
+ *             i.e. Fortran xb(ens, n, 1-halo:num_lat+halo, 1-halo:num_lon+halo)
+ *   axb, axa: double [n][num_lat + 2*halo][num_lon + 2*halo], n fastest
+ * Only interior points of xa/axa are written; halo points are left untouched.
+ * "lat" is the reference's x direction (nx), "lon" its y direction (ny).
+ *
+ * Threading: one context per host thread; calls on one context are serialised
+ * by the caller.  The context owns all device buffers.
+ */
+#ifndef LETKF_GPU_H_
+#define LETKF_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LG_MAX_VARS 16       /* DA variables (ps,u,v,pt,...) */
+#define LG_MAX_OBS_TYPES 16  /* observation types (AIRCAR, SATWND, ...) */
+#define LG_MAX_OBS_VARS 8    /* variables per observation type */
+
+/* status codes */
+#define LG_OK 0
+#define LG_ERR_ARG -1           /* null pointer / bad argument */
+#define LG_ERR_SHAPE -2         /* inconsistent sizes */
+#define LG_ERR_UNSUPPORTED -3   /* option combination not implemented */
+#define LG_ERR_NAN -4           /* NaN found in the background (module_da_parallel.F90:190-193) */
+#define LG_ERR_OBS_OUTSIDE -5   /* obs outside its block's grid (letkf_obs.F90:211-231) */
+#define LG_ERR_VARNAME -6       /* obs variable not among DA variables (letkf_obs.F90:113-117) */
+#define LG_ERR_EIG -7           /* eigensolver did not converge (letkf_core.F90:119-122) */
+#define LG_ERR_CUDA -8          /* CUDA runtime error */
+#define LG_ERR_NOMEM -9         /* device or host allocation failed */
+#define LG_ERR_STATE -10        /* call order violated (grid/obs not set) */
+#define LG_ERR_TIMEOUT -11      /* a bounded device wait ran out */
+
+/* precision of the analysis */
+#define LG_PREC_FP64 0   /* plain FP64 everywhere (parity path) */
+#define LG_PREC_MIXED 1  /* BF16 hi/lo tensor-core contractions, FP64 eigensolve */
+
+/* vertical coordinate (da_vert_coord_init scheme) */
+#define LG_VCOORD_HYBRID 0  /* ph = a*(p0-ptop) + b*(ps-ptop) + ptop */
+#define LG_VCOORD_SIGMA 1   /* ph = a*(ps-ptop) + ptop  (ptop = pt) */
+
+/* Mirrors the namelist_da / namelist_total fields letkf_init reads
+ * (letkf_init.F90:27-81, da_namelist_mod.F90:79-89). */
+typedef struct lg_config {
+  int ens;             /* ensemble size k (svr_ensemble) */
+  int num_lat;         /* global latitudes (reference nx direction) */
+  int num_lon;         /* global longitudes (reference ny direction) */
+  int nz;              /* model levels (num_lev) */
+  int halo;            /* da_halo, >= 1 */
+  int n_var;           /* DA variables, 2-D ones first (var_info ordering) */
+  int var_lev[LG_MAX_VARS]; /* 1 for a 2-D variable, nz for a 3-D one */
+  int ps_index;        /* 1-based row of surface pressure in n (ps_pos) */
+  double local_dist;   /* da_loc_distance [km] */
+  double vert_dist;    /* da_vert_distance [ln p]; <= 0 selects the 2-D path */
+  double inflation;    /* da_inflation_factor (rho) */
+  double obs_polar;    /* obs with |lat| > obs_polar are dropped (91 = keep all) */
+  int gc_filter;       /* da_gc_enable: Gaspari-Cohn (1) or box (0) horizontally */
+  int gc_filter_vertical; /* da_gc_enable_vertical */
+  int max_obs;         /* MAX_OBS cap on local entries per column; 0 = no cap */
+  int global_nx;       /* virtual decomposition: blocks in latitude */
+  int global_ny;       /* virtual decomposition: blocks in longitude */
+  int cube_n;          /* da_block_interval; only 1 is supported */
+  int cube_nz;         /* da_vertical_interval; only 1 is supported */
+  int overlap;         /* da_block_overlap; only 0 is supported */
+  int precision;       /* LG_PREC_FP64 or LG_PREC_MIXED */
+  int vcoord;          /* LG_VCOORD_HYBRID or LG_VCOORD_SIGMA */
+} lg_config;
+
+/* One observation type: a fixed (levels x variables) record shape
+ * (read_obs_mod.F90:15-27, 99-146). */
+typedef struct lg_obs_type {
+  int nz;                      /* obs_nz: levels per observation */
+  int nvar;                    /* obs_nvar: variables per level */
+  int var[LG_MAX_OBS_VARS];    /* 0-based DA variable index of each obs variable */
+} lg_obs_type;
+
+/* Structure-of-arrays observation set for the whole globe.  It replaces the
+ * Redis observation store plus comm_obs_data: the library builds every virtual
+ * block's observation list from it with the Redis box-query semantics
+ * (redis_wrapper.c:4158-4296: inclusive lon/lat bounds printed with %.5f,
+ * result ordered by observation index).  Observation o has type type[o]; its
+ * nz levels occupy ph[ph_off(o) .. +nz) and its nz*nvar values occupy
+ * yo/rinv[val_off(o) .. +nz*nvar) in (var fastest, level slowest) order, where
+ * the offsets are the running sums over o' < o. */
+typedef struct lg_obs_soa {
+  int n_types;
+  const lg_obs_type* types; /* n_types */
+  int n_obs;
+  const int* type;          /* n_obs */
+  const double* lat;        /* n_obs, degrees (float-valued in the reference) */
+  const double* lon;        /* n_obs, degrees in [0, 360) */
+  const double* ph;         /* sum of nz over obs: observation pressure [Pa] */
+  const double* yo;         /* sum of nz*nvar over obs: observed (perturbed) values */
+  const double* rinv;       /* sum of nz*nvar over obs: 1/sigma^2 */
+} lg_obs_soa;
+
+typedef struct lg_stats {
+  int64_t n_columns;        /* analysed grid columns */
+  int64_t n_solves;         /* letkf_core solves */
+  int64_t n_copies;         /* block-observation copies (obs counted once per block box) */
+  int64_t n_entries;        /* (copy, level, var) entries with H(x) */
+  int64_t nobsl_total;      /* sum over columns of local entries */
+  int64_t nobsl_max;        /* max local entries of one column */
+  int64_t n_capped;         /* columns truncated at max_obs */
+  int64_t n_band;           /* candidate pairs with |ri-2| < 1e-12 (decision sensitive to libm ulps) */
+  int64_t n_eig_fail;       /* eigensolves that hit the sweep limit */
+  double ms_hx, ms_search, ms_solve, ms_total; /* last lg_run phase times (device events) */
+} lg_stats;
+
+typedef struct lg_ctx lg_ctx;
+
+/* Create a context on the current CUDA device.  Validates the configuration. */
+int lg_create(lg_ctx** ctx, const lg_config* cfg);
+
+/* Model grid and vertical coordinate.
+ * grid_lat: num_lat+1 floats (REAL(4) as in pro_info.F90:11-12); entry num_lat is forced to 90.
+ * grid_lon: num_lon+1 floats; entry num_lon is forced to 360 (pro_info.F90:77-83).
+ * coef_a, coef_b: nz+1 doubles: hybrid hyai/hybi, or sigma sigi (coef_b unused).
+ * p0, ptop: hybrid reference and top pressure [Pa]; sigma uses ptop as pt. */
+int lg_set_grid(lg_ctx* ctx, const float* grid_lat, const float* grid_lon,
+                const double* coef_a, const double* coef_b, double p0, double ptop);
+
+/* Observations for the next analysis (host arrays, copied). */
+int lg_set_obs(lg_ctx* ctx, const lg_obs_soa* obs);
+
+/* One complete analysis, host arrays (letkf_run).  ntimes is the DA cycle index;
+ * it selected the Redis time slot in the reference and is recorded only. */
+int lg_run(lg_ctx* ctx, int ntimes, const double* xb, const double* axb, double* xa, double* axa);
+
+/* Same with device pointers on the context's stream (cudaStream_t passed as void*,
+ * NULL = legacy default stream). */
+int lg_run_device(lg_ctx* ctx, int ntimes, const double* d_xb, const double* d_axb,
+                  double* d_xa, double* d_axa, void* stream);
+
+/* Statistics of the last lg_run. */
+int lg_get_stats(const lg_ctx* ctx, lg_stats* st);
+
+/* Neighbour lists of the last analysis (device-built), for parity checks.
+ * counts: num_lat*num_lon ints, column c = (lon-1)*num_lat + (lat-1);
+ * entries/rloc: total local entries in column order; entries hold the global
+ * copy-entry index (see lg_copy_layout).  Pass NULL arrays to query the total
+ * through *total only. */
+int lg_get_lists(const lg_ctx* ctx, int* counts, int* entries, double* rloc, int64_t* total);
+
+/* Layout of block-observation copies built by lg_set_obs: for each copy j
+ * (ordered by block b = (by-1)*global_nx + (bx-1), then type, then observation
+ * index), copy_obs[j] = observation index, copy_block[j] = b, and
+ * copy_entry_off[j] = first copy-entry index (n_copies+1 values). */
+int lg_copy_layout(const lg_ctx* ctx, int* copy_obs, int* copy_block,
+                   int64_t* copy_entry_off, int64_t* n_copies);
+
+/* H(x) of the last analysis: yb[n_entries][ens] (member fastest) and
+ * dis[n_entries] per copy entry, after mean removal (letkf_obs.F90:156-183). */
+int lg_get_hx(const lg_ctx* ctx, double* yb, double* dis);
+
+void lg_destroy(lg_ctx* ctx);
+
+/* Column-batched letkf_core on device arrays (letkf_core.F90:14-233):
+ * for batch b with p_b = nobsl[b] entries starting at offset off[b]:
+ *   hxens[(off[b]+j)*ens + i], rdiaginv[off[b]+j] (float), dep[off[b]+j], rloc[off[b]+j]
+ *   -> trans[b*ens*ens + i + ens*j] (column-major ens x ens), wbar[b*ens + i].
+ * precision: LG_PREC_FP64 or LG_PREC_MIXED.  stream: cudaStream_t or NULL. */
+int lg_core_batch(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
+                  const double* d_hxens, const float* d_rdiaginv, const double* d_dep,
+                  const double* d_rloc, double inflation, int precision,
+                  double* d_trans, double* d_wbar, void* stream);
+
+/* Fortran drop-in for the external letkf_core (all arguments by reference, host
+ * arrays), so a build of the reference links this instead of its own letkf_core.
+ * pflag is accepted and ignored.  Errors are reported through *ierr when the
+ * caller passes the optional 11th argument through the lg_letkf_core variant. */
+void letkf_core_(const int* nanals, const int* nobsl, const double* hxens,
+                 const float* rdiaginv, const double* dep, const double* rloc,
+                 double* trans, double* overline_w, const double* inflation_factor,
+                 const int* pflag);
+
+/* letkf_core_ with a status result. */
+int lg_letkf_core(int nanals, int nobsl, const double* hxens, const float* rdiaginv,
+                  const double* dep, const double* rloc, double* trans,
+                  double* overline_w, double inflation_factor);
+
+/* Human-readable name of a status code. */
+const char* lg_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LETKF_GPU_H_ */

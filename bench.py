@@ -1,0 +1,360 @@
+#!/usr/bin/env python
+"""LETKF analysis benchmark on GB300: grid columns per second.
+
+One "step" is one complete LETKF analysis (H(x) of every member, per-column
+local observation search, one solve per column and level, Xa update) of the
+synthetic workload named by --config (default cfg3: 360x180x32, ps/u/v/pt,
+N=64, 1e6 observations, Gaspari-Cohn 800 km + 0.2 ln p, rho 1.05).
+
+value : columns / (device time of one analysis) with the background already
+        resident in HBM (lg_run_device), CUDA events on the launching stream.
+e2e   : the same metric through the host-array call a DA driver makes
+        (lg_set_obs + lg_run with pinned host buffers: observation ingest and the
+        background H2D copy, analysis D2H copy inside the timed region).
+cpu_baseline / --impl reference : the CPU oracle (C restatement of the
+        reference's Fortran hot path; the Fortran itself cannot be built here)
+        on the host cores, over a bounded sample of columns, extrapolated.
+
+Inputs (3.4 GB background for cfg3) exceed the 129 MB L2, so no flush is done
+between steps.  For --gpus N > 1 (torchrun) every rank analyses its own full
+replica of the workload ("replicas only": the single-GPU analysis holds the
+whole globe); value is the sum of columns over ranks / max step time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "dida-thhpca_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "LETKF grid columns/s, mixed vs plain FP64 on one GB300 at <=1e-4 rel RMS"
+UNIT = "columns/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cfg3")
+    ap.add_argument("--precision", default=None, choices=[None, "fp64", "mixed"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="target CPU time of the bounded oracle sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def fp64_peak_tflops(torch, dev):
+    """cuBLAS DGEMM throughput, the FP64 denominator for the FP64-bound kernels."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    best = 1e30
+    for _ in range(3):
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def cpu_sample(cfg, obs, xb, axb, seconds, nthreads):
+    """Oracle timing on a bounded sample: H(x) of every observation, then columns
+    from the equator band until ~seconds elapse; returns columns/s for a full
+    analysis (H(x) + all columns at the sampled rate)."""
+    import numpy as np
+    from oracle import oracle as orc
+
+    o = orc.Oracle(cfg, obs)
+    t0 = time.perf_counter()
+    o.hx(xb, axb, nthreads)
+    t_hx = time.perf_counter() - t0
+    ncol = cfg.num_lat * cfg.num_lon
+    xa = np.zeros_like(xb)
+    axa = np.zeros_like(axb)
+    start = cfg.num_lat // 2 + cfg.num_lat * (cfg.num_lon // 3)
+    done, t_cols, chunk = 0, 0.0, max(1, nthreads)
+    while t_cols < seconds and done < ncol:
+        c0 = (start + done) % ncol
+        c1 = min(ncol, c0 + chunk)
+        t0 = time.perf_counter()
+        o.analysis(xb, axb, xa, axa, c0, c1, nthreads)
+        t_cols += time.perf_counter() - t0
+        done += c1 - c0
+        chunk = min(4 * chunk, max(nthreads, int(done / max(t_cols, 1e-6) * (seconds - t_cols)) + 1))
+    t_full = t_hx + t_cols * ncol / done
+    return ncol / t_full, {
+        "sample": f"H(x) of all {obs.n_obs} obs ({t_hx:.2f} s) + {done} of {ncol} columns "
+                  f"({t_cols:.2f} s), extrapolated to the full analysis",
+        "lapack": "OpenBLAS dgemm/dsyevd" if orc.lapack_loaded() else "built-in loops + Jacobi"}
+
+
+def reference_arm(args):
+    """--impl reference: the CPU oracle port on all host cores, same workload."""
+    import numpy as np
+    import letkf_gb300 as lg
+    import synth
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cfg = lg.preset(args.config)
+    t0 = time.perf_counter()
+    w = synth.make_workload(cfg)
+    nthreads = os.cpu_count() or 1
+    per_step = max(2.0, 120.0 / max(1, args.steps + args.warmup))
+    vals = []
+    info = {}
+    for i in range(args.warmup + args.steps):
+        v, info = cpu_sample(cfg, w.obs, np.ascontiguousarray(w.xb), np.ascontiguousarray(w.axb),
+                             per_step, nthreads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cfg.num_lat * cfg.num_lon / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded spherical-harmonic ensemble, uniform observations)",
+        "config": {"workload": f"{cfg.name}: {cfg.num_lon}x{cfg.num_lat}x{cfg.nz}, N={cfg.ens}, "
+                               f"{cfg.n_obs} obs, L={cfg.local_dist:g} km"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": info["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "C restatement of the reference's Fortran letkf_run (no Fortran compiler, MPI or "
+                "Redis on this image); " + info["lapack"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import numpy as np
+    import torch
+
+    import letkf_gb300 as lg
+    import synth
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import lg_build
+    lg_build.build()
+
+    cfg = lg.preset(args.config)
+    if args.precision:
+        cfg = cfg.replace(precision=lg.LG_PREC_MIXED if args.precision == "mixed" else lg.LG_PREC_FP64)
+    w = synth.make_workload(cfg, backend="torch", device=dev)
+    ncol = cfg.num_lat * cfg.num_lon
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    xb, axb = w.xb.contiguous(), w.axb.contiguous()
+    xa = torch.zeros_like(xb)
+    axa = torch.zeros_like(axb)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        ctx.letkf_run_device(0, xb, axb, xa, axa, stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    acc = {"ms_gram": 0.0, "ms_eig": 0.0, "ms_hx": 0.0, "ms_search": 0.0, "n_launches": 0,
+           "n_gram_entries": 0}
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+        st = ctx.stats()
+        for key in acc:
+            acc[key] += st[key]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * ncol / (ms * 1e-3)
+    st = ctx.stats()
+
+    # roofline of the dominant kernel (per-launch averages over the timed steps)
+    peaks = measured_peaks()
+    k = cfg.ens
+    gram_flops = 2.0 * acc["n_gram_entries"] * k * k + 2.0 * acc["n_gram_entries"] * k
+    nchunk_launches = max(1, (acc["n_launches"] - 5 * args.steps) // 2)
+    solves = st["n_solves"] * args.steps
+    eig_flops = solves * (4.0 * k ** 3 + 2.0 * k ** 3)  # tridiagonal+QL nominal 4k^3, sqrt 2k^3
+    fp64_peak = fp64_peak_tflops(torch, dev)
+    kernels = {
+        "gram": {"ms": acc["ms_gram"], "flops": gram_flops,
+                 "bound": "tensor" if cfg.precision == lg.LG_PREC_MIXED else "fp64"},
+        "eig_update": {"ms": acc["ms_eig"], "flops": eig_flops, "bound": "fp64"},
+    }
+    dom_name = max(kernels, key=lambda n: kernels[n]["ms"])
+    dom = kernels[dom_name]
+    if dom["bound"] == "tensor":
+        peak, peak_src = peaks.get("bf16_tflops", 1900.0), "bf16 burst, MEASURED_PEAKS.json"
+    else:
+        peak, peak_src = fp64_peak, "cuBLAS DGEMM measured in this run"
+    achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12 if dom["ms"] > 0 else 0.0
+    roofline = {"bound": dom["bound"], "kernel": dom_name, "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": peak_src,
+                "share_of_step": dom["ms"] / (ms * args.steps)}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16/f32 contractions, f64 eig" if cfg.precision == lg.LG_PREC_MIXED else "f64",
+        "data": "synthetic (seeded spherical-harmonic ensemble, uniform observations)",
+        "config": {"workload": f"{cfg.name}: {cfg.num_lon}x{cfg.num_lat}x{cfg.nz}, ps/u/v/pt, "
+                               f"N={cfg.ens}, {cfg.n_obs} obs, L={cfg.local_dist:g} km, "
+                               f"vert {cfg.vert_dist:g} ln p, rho={cfg.inflation}",
+                   "precision": "mixed" if cfg.precision == lg.LG_PREC_MIXED else "fp64",
+                   "columns": ncol, "solves_per_step": st["n_solves"],
+                   "local_entries_per_step": st["nobsl_total"],
+                   "l2": "inputs (background 3.4 GB) larger than L2; no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "clocks": clocks,
+        "gpu_launches": acc["n_launches"],
+        "phases_ms": {"hx": acc["ms_hx"] / args.steps, "search": acc["ms_search"] / args.steps,
+                      "gram": acc["ms_gram"] / args.steps, "eig_update": acc["ms_eig"] / args.steps},
+        "roofline": roofline,
+        "fp64_peak_tflops": fp64_peak,
+    }
+
+    # end to end through the host-array C ABI call
+    if not args.no_e2e and rank == 0:
+        hxb = torch.empty(xb.shape, dtype=torch.float64, pin_memory=True)
+        haxb = torch.empty(axb.shape, dtype=torch.float64, pin_memory=True)
+        hxa = torch.zeros(xb.shape, dtype=torch.float64, pin_memory=True)
+        haxa = torch.zeros(axb.shape, dtype=torch.float64, pin_memory=True)
+        hxb.copy_(xb)
+        haxb.copy_(axb)
+        nxb, naxb, nxa, naxa = (t.numpy() for t in (hxb, haxb, hxa, haxa))
+        ctx.set_obs(w.obs)
+        ctx.letkf_run(0, nxb, naxb, nxa, naxa)
+        ts = []
+        for _ in range(args.e2e_steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ctx.set_obs(w.obs)
+            ctx.letkf_run(0, nxb, naxb, nxa, naxa)
+            ts.append(time.perf_counter() - t0)
+        o = w.obs
+        h2d = nxb.nbytes + naxb.nbytes + sum(a.nbytes for a in (o.type, o.lat, o.lon, o.ph, o.yo, o.rinv))
+        h = cfg.halo
+        d2h = (nxa[h:-h, h:-h].nbytes + naxa[h:-h, h:-h].nbytes)
+        line["e2e"] = {"value": ncol / min(ts), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                       "d2h_bytes_per_step": int(d2h)}
+
+    if not args.no_cpu_baseline and rank == 0:
+        xb_h = xb.cpu().numpy()
+        axb_h = axb.cpu().numpy()
+        nthreads = os.cpu_count() or 1
+        v, info = cpu_sample(cfg, w.obs, xb_h, axb_h, args.cpu_seconds, nthreads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                                "sample": info["sample"] + "; " + info["lapack"]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.letkf_final()
+    if dist:
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

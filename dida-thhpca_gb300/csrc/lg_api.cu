@@ -66,6 +66,8 @@ struct lg_ctx {
   size_t state_elems = 0;
   lg_stats stats{};
   cudaEvent_t ev[5] = {};
+  std::vector<cudaEvent_t> kev;  // per-launch events of the solve phase
+  unsigned long long* d_work = nullptr;
 };
 
 namespace {
@@ -331,7 +333,8 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   c->x_res = g.num_lat % g.global_nx;
   c->y_sec = g.num_lon / g.global_ny;
   c->y_res = g.num_lon % g.global_ny;
-  if (dalloc(&c->d_status, 4) != LG_OK || dalloc(&c->d_band, 1) != LG_OK) {
+  if (dalloc(&c->d_status, 4) != LG_OK || dalloc(&c->d_band, 1) != LG_OK ||
+      dalloc(&c->d_work, 1) != LG_OK) {
     lg_destroy(c);
     return LG_ERR_NOMEM;
   }
@@ -569,15 +572,19 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   }
   CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * 4, st));
   CK(cudaMemsetAsync(c->d_band, 0, sizeof(unsigned long long), st));
+  CK(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), st));
+  int64_t launches = 0;
   CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
   CK(cudaEventRecord(c->ev[0], st));
   // H(x)
   lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, st);
+  launches += c->obs.n_copies > 0;
   CK(cudaGetLastError());
   CK(cudaEventRecord(c->ev[1], st));
   // selection: count, scan, fill
   lg::launch_search(geo, c->obs, c->lists, 0, c->d_band, st);
   lg::launch_scan_counts(c->lists.cnt, c->lists.off, ncol, c->d_scan_tmp, c->scan_tmp_bytes, st);
+  launches += 3;  // count pass + the scan's init and scan kernels
   int64_t total = 0;
   CK(cudaMemcpyAsync(&total, c->lists.off + ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -593,6 +600,7 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   }
   c->list_total = total;
   lg::launch_search(geo, c->obs, c->lists, 1, nullptr, st);
+  launches += 1;
   CK(cudaGetLastError());
   CK(cudaEventRecord(c->ev[2], st));
   // solves, in column chunks bounded by the Gram workspace
@@ -609,24 +617,46 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
     }
     c->solve_cap = cap;
   }
-  for (int c0 = 0; c0 < ncol; c0 += chunk) {
+  const int nchunks = (ncol + chunk - 1) / chunk;
+  while ((int)c->kev.size() < 3 * nchunks) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    c->kev.push_back(e);
+  }
+  for (int q = 0; q < nchunks; ++q) {
+    const int c0 = q * chunk;
     lg::SolveBatch b{};
     b.mode = 0;
     b.first_col = c0;
     b.ncols = std::min(chunk, ncol - c0);
     b.levels = levels;
     b.nsolves = b.ncols * levels;
+    b.work = c->d_work;
+    CK(cudaEventRecord(c->kev[3 * q], st));
     lg::launch_gram64(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, st);
+    CK(cudaEventRecord(c->kev[3 * q + 1], st));
     lg::launch_eig_apply(geo, b, c->d_C, c->d_t, xb, axb, xa, axa, nullptr, nullptr,
                          c->d_status + 1, st);
+    CK(cudaEventRecord(c->kev[3 * q + 2], st));
+    launches += 2;
   }
   CK(cudaGetLastError());
   CK(cudaEventRecord(c->ev[3], st));
   int status[4];
-  unsigned long long band = 0;
+  unsigned long long band = 0, work = 0;
   CK(cudaMemcpyAsync(status, c->d_status, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&band, c->d_band, sizeof(band), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&work, c->d_work, sizeof(work), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  for (int q = 0; q < nchunks; ++q) {
+    float a = 0.f, b2 = 0.f;
+    cudaEventElapsedTime(&a, c->kev[3 * q], c->kev[3 * q + 1]);
+    cudaEventElapsedTime(&b2, c->kev[3 * q + 1], c->kev[3 * q + 2]);
+    S.ms_gram += a;
+    S.ms_eig += b2;
+  }
+  S.n_launches = launches;
+  S.n_gram_entries = (int64_t)work;
   float ms;
   cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); S.ms_hx = ms;
   cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); S.ms_search = ms;
@@ -733,6 +763,8 @@ void lg_destroy(lg_ctx* c) {
   dfree(c->d_xb); dfree(c->d_axb); dfree(c->d_xa); dfree(c->d_axa);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : c->kev) cudaEventDestroy(e);
+  dfree(c->d_work);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
 }

@@ -91,6 +91,7 @@ __global__ void __launch_bounds__(kGramThreads) gram64_kernel(Geometry g, HxDev 
   double tacc = 0.0;  // t_i for i = tid (tid < k)
 
   int scan = 0;
+  int nproc = 0;
   while (true) {
     // warp 0 refills the queue with nonzero-weight entries
     if (tid < 32) {
@@ -132,6 +133,7 @@ __global__ void __launch_bounds__(kGramThreads) gram64_kernel(Geometry g, HxDev 
     const int qn = q_n;
     if (qn == 0) break;
     const int nt = qn < kTE ? qn : kTE;
+    nproc += nt;
     // stage the tile: ytile[e][i] = y_e[i] * rr_e, rd[e] = rr_e * d_e
     for (int idx = tid; idx < kTE * kp; idx += kGramThreads) {
       const int e = idx / kp, i = idx - e * kp;
@@ -202,6 +204,7 @@ __global__ void __launch_bounds__(kGramThreads) gram64_kernel(Geometry g, HxDev 
       }
   }
   if (tid < k) tout[(size_t)s * k + tid] = tacc;
+  if (b.work && tid == 0) atomicAdd(b.work, (unsigned long long)nproc);
 }
 
 void launch_gram64(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,

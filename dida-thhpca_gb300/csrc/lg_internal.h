@@ -97,6 +97,7 @@ struct SolveBatch {
   const float* b_rdiag;
   const double* b_dep;
   const double* b_rloc;
+  unsigned long long* work;  // optional: += nonzero-weight entries processed
 };
 
 // kernels (host launchers), all asynchronous on `stream`

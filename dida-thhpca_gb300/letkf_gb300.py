@@ -70,7 +70,8 @@ class LgStats(C.Structure):
         ("n_entries", C.c_int64), ("nobsl_total", C.c_int64), ("nobsl_max", C.c_int64),
         ("n_capped", C.c_int64), ("n_band", C.c_int64), ("n_eig_fail", C.c_int64),
         ("ms_hx", C.c_double), ("ms_search", C.c_double), ("ms_solve", C.c_double),
-        ("ms_total", C.c_double),
+        ("ms_total", C.c_double), ("ms_gram", C.c_double), ("ms_eig", C.c_double),
+        ("n_launches", C.c_int64), ("n_gram_entries", C.c_int64),
     ]
 
     def as_dict(self):

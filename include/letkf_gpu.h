@@ -133,6 +133,10 @@ typedef struct lg_stats {
   int64_t n_band;           /* candidate pairs with |ri-2| < 1e-12 (decision sensitive to libm ulps) */
   int64_t n_eig_fail;       /* eigensolves that hit the sweep limit */
   double ms_hx, ms_search, ms_solve, ms_total; /* last lg_run phase times (device events) */
+  double ms_gram;           /* sum of Gram-kernel launch durations of the last lg_run */
+  double ms_eig;            /* sum of eigensolve+update launch durations */
+  int64_t n_launches;       /* kernels this library launched in the last lg_run */
+  int64_t n_gram_entries;   /* sum over solves of nonzero-weight entries (Gram work) */
 } lg_stats;
 
 typedef struct lg_ctx lg_ctx;

@@ -153,7 +153,7 @@ def cpu_sample(cfg, obs, xb, axb, seconds, nthreads):
     done, t_cols, chunk = 0, 0.0, max(1, nthreads)
     while t_cols < seconds and done < ncol:
         c0 = (start + done) % ncol
-        c1 = min(ncol, c0 + chunk)
+        c1 = min(ncol, c0 + min(chunk, ncol - done))
         t0 = time.perf_counter()
         o.analysis(xb, axb, xa, axa, c0, c1, nthreads)
         t_cols += time.perf_counter() - t0

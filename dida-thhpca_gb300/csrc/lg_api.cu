@@ -58,6 +58,12 @@ struct lg_ctx {
   // solve workspace
   double *d_C = nullptr, *d_t = nullptr;
   size_t solve_cap = 0;
+  // lane-parallel eigensolver scratch (tridiagonal form, eigenvalues, rotation log)
+  double *d_tri = nullptr, *d_lam = nullptr;
+  double2* d_rot_cs = nullptr;
+  unsigned char* d_rot_i = nullptr;
+  int *d_rot_n = nullptr, *d_ovf_list = nullptr;
+  int rot_cap = 0;
   // status words: [0] err, [1] eig_fail
   int* d_status = nullptr;
   unsigned long long* d_band = nullptr;
@@ -605,13 +611,28 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   CK(cudaEventRecord(c->ev[2], st));
   // solves, in column chunks bounded by the Gram workspace
   const int levels = g.vert_dist > 0.0 ? g.nz : 1;
-  const size_t per_col = (size_t)levels * k * k;
-  int chunk = (int)std::min<size_t>((size_t)ncol, std::max<size_t>(1, ((size_t)256 << 20) / per_col));
+  const size_t per_col = (size_t)levels * k * k * sizeof(double);
+  int chunk = (int)std::min<size_t>((size_t)ncol, std::max<size_t>(1, ((size_t)1 << 30) / per_col));
+  const bool use_eig2 = lg::eig2_supported(geo);
   if ((size_t)chunk * levels > c->solve_cap) {
-    dfree(c->d_C);
-    dfree(c->d_t);
+    dfree(c->d_C); dfree(c->d_t); dfree(c->d_tri); dfree(c->d_lam); dfree(c->d_rot_cs);
+    dfree(c->d_rot_i); dfree(c->d_rot_n); dfree(c->d_ovf_list);
     const size_t cap = (size_t)chunk * levels;
-    if (dalloc(&c->d_C, cap * k * k) != LG_OK || dalloc(&c->d_t, cap * k) != LG_OK) {
+    c->rot_cap = 3 * k * k;
+    // test hook: a small log forces the overflow fallback path
+    if (const char* env = getenv("LETKF_GB300_ROT_CAP")) c->rot_cap = std::max(1, atoi(env));
+    int r = LG_OK;
+    r |= dalloc(&c->d_C, cap * k * k);
+    r |= dalloc(&c->d_t, cap * k);
+    if (use_eig2) {
+      r |= dalloc(&c->d_tri, cap * lg::eig2_tri_doubles(k));
+      r |= dalloc(&c->d_lam, cap * k);
+      r |= dalloc(&c->d_rot_cs, cap * (size_t)c->rot_cap);
+      r |= dalloc(&c->d_rot_i, cap * (size_t)c->rot_cap);
+      r |= dalloc(&c->d_rot_n, cap);
+      r |= dalloc(&c->d_ovf_list, cap);
+    }
+    if (r != LG_OK) {
       c->solve_cap = 0;
       return LG_ERR_NOMEM;
     }
@@ -633,12 +654,30 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
     b.nsolves = b.ncols * levels;
     b.work = c->d_work;
     CK(cudaEventRecord(c->kev[3 * q], st));
-    lg::launch_gram64(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, st);
+    if (g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k))
+      lg::launch_gram_tc(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, c->d_status, st);
+    else
+      lg::launch_gram64(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, st);
     CK(cudaEventRecord(c->kev[3 * q + 1], st));
-    lg::launch_eig_apply(geo, b, c->d_C, c->d_t, xb, axb, xa, axa, nullptr, nullptr,
-                         c->d_status + 1, st);
+    if (use_eig2) {
+      CK(cudaMemsetAsync(c->d_status + 2, 0, sizeof(int), st));
+      lg::launch_eig2(geo, b, c->d_C, c->d_t, xb, axb, xa, axa, c->d_tri, c->d_lam, c->d_rot_cs,
+                      c->d_rot_i, c->d_rot_n, c->rot_cap, c->d_ovf_list, c->d_status + 2,
+                      c->d_status + 1, st);
+      // matrices whose rotation log overflowed: accumulate-eigenvector solver
+      lg::SolveBatch fb = b;
+      fb.solve_list = c->d_ovf_list;
+      fb.solve_count = c->d_status + 2;
+      lg::launch_eig_apply(geo, fb, c->d_C, c->d_t, xb, axb, xa, axa, nullptr, nullptr,
+                           c->d_status + 1, st);
+      launches += 4;
+    } else {
+      lg::launch_eig_apply(geo, b, c->d_C, c->d_t, xb, axb, xa, axa, nullptr, nullptr,
+                           c->d_status + 1, st);
+      launches += 1;
+    }
     CK(cudaEventRecord(c->kev[3 * q + 2], st));
-    launches += 2;
+    launches += 1;
   }
   CK(cudaGetLastError());
   CK(cudaEventRecord(c->ev[3], st));
@@ -760,6 +799,8 @@ void lg_destroy(lg_ctx* c) {
   dfree(c->lists.capped);
   if (c->d_scan_tmp) cudaFree(c->d_scan_tmp);
   dfree(c->d_C); dfree(c->d_t); dfree(c->d_status); dfree(c->d_band);
+  dfree(c->d_tri); dfree(c->d_lam); dfree(c->d_rot_cs); dfree(c->d_rot_i); dfree(c->d_rot_n);
+  dfree(c->d_ovf_list);
   dfree(c->d_xb); dfree(c->d_axb); dfree(c->d_xa); dfree(c->d_axa);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -803,7 +844,10 @@ int lg_core_batch(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
   cudaMemsetAsync(fail, 0, sizeof(int), st);
   lg::HxDev hx{};
   lg::ListDev l{};
-  lg::launch_gram64(geo, hx, l, b, nullptr, C, t, st);
+  if (precision == LG_PREC_MIXED && lg::gram_tc_supported(ens))
+    lg::launch_gram_tc(geo, hx, l, b, nullptr, C, t, fail, st);
+  else
+    lg::launch_gram64(geo, hx, l, b, nullptr, C, t, st);
   lg::launch_eig_apply(geo, b, C, t, nullptr, nullptr, nullptr, nullptr, d_trans, d_wbar, fail, st);
   int h_fail = 0;
   if (cudaGetLastError() != cudaSuccess ||

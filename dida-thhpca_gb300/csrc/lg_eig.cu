@@ -15,6 +15,8 @@
 // V (f .* (V^T x)), which costs 4k^2 per row instead of k^3.
 #include <float.h>
 
+#include <algorithm>
+
 #include "lg_device.cuh"
 #include "lg_internal.h"
 
@@ -48,7 +50,15 @@ __global__ void __launch_bounds__(NT) eig_apply_kernel(Geometry g, SolveBatch b,
                                                        double* axa, double* trans_out,
                                                        double* wbar_out, int* eig_fail) {
   using B = Blk<NT>;
-  const int s = blockIdx.x;
+  for (int ii = blockIdx.x;; ii += gridDim.x) {
+  int s;
+  if (b.solve_list) {
+    if (ii >= *b.solve_count) return;
+    s = b.solve_list[ii];
+  } else {
+    if (ii >= b.nsolves) return;
+    s = ii;
+  }
   const int n = g.ens;
   const int LD = n | 1;  // odd row stride
   const int tid = threadIdx.x;
@@ -194,15 +204,16 @@ __global__ void __launch_bounds__(NT) eig_apply_kernel(Geometry g, SolveBatch b,
         int brk = 0;
         if (tid == 0) {
           const double f = sn * e[i], bb = cs * e[i];
-          const double r = hypot(f, gv);
+          const double r = sqrt(f * f + gv * gv);
           e[i + 1] = r;
           if (r == 0.0) {
             d[i + 1] -= pp;
             e[m] = 0.0;
             brk = 1;
           } else {
-            sn = f / r;
-            cs = gv / r;
+            const double rinv = 1.0 / r;
+            sn = f * rinv;
+            cs = gv * rinv;
             gv = d[i + 1] - pp;
             const double rr = (d[i] - gv) * sn + 2.0 * cs * bb;
             pp = sn * rr;
@@ -270,6 +281,8 @@ __global__ void __launch_bounds__(NT) eig_apply_kernel(Geometry g, SolveBatch b,
   }
   __syncthreads();
   if (s_fail && tid == 0) atomicAdd(eig_fail, 1);
+  __syncthreads();
+  if (tid == 0) s_fail = 0;
 
   if (b.mode == 1) {
     // explicit trans(i, j) = W(i, j) + overline_w(i), column-major
@@ -282,7 +295,8 @@ __global__ void __launch_bounds__(NT) eig_apply_kernel(Geometry g, SolveBatch b,
       }
       wbar_out[(size_t)s * n + i] = wb[i];
     }
-    return;
+    __syncthreads();
+    continue;
   }
 
   // rows owned by this solve
@@ -335,6 +349,8 @@ __global__ void __launch_bounds__(NT) eig_apply_kernel(Geometry g, SolveBatch b,
     if (tid == 0) axa[r + (size_t)g.n * ci] = mean;
     __syncthreads();
   }
+  __syncthreads();
+  }  // solves of this CTA
 }
 
 void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
@@ -344,18 +360,17 @@ void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, c
   const int n = g.ens;
   const int LD = n | 1;
   const size_t smem = sizeof(double) * ((size_t)n * LD + 6 * n + 8);
-  if (n <= 32) {
-    eig_apply_kernel<32><<<b.nsolves, 32, smem, stream>>>(g, b, C, t, xb, axb, xa, axa, trans,
-                                                          wbar, eig_fail);
-  } else if (n <= 64) {
-    cudaFuncSetAttribute(eig_apply_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  const int grid = b.solve_list ? std::min(b.nsolves, 152 * 6) : b.nsolves;
+  if (n <= 64) {
+    // one warp per matrix: the QL rotations are broadcast by shuffles, no block barriers
+    cudaFuncSetAttribute(eig_apply_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
-    eig_apply_kernel<64><<<b.nsolves, 64, smem, stream>>>(g, b, C, t, xb, axb, xa, axa, trans,
+    eig_apply_kernel<32><<<grid, 32, smem, stream>>>(g, b, C, t, xb, axb, xa, axa, trans,
                                                           wbar, eig_fail);
   } else {
     cudaFuncSetAttribute(eig_apply_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
-    eig_apply_kernel<128><<<b.nsolves, 128, smem, stream>>>(g, b, C, t, xb, axb, xa, axa,
+    eig_apply_kernel<128><<<grid, 128, smem, stream>>>(g, b, C, t, xb, axb, xa, axa,
                                                             trans, wbar, eig_fail);
   }
 }

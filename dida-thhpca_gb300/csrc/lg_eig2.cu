@@ -1,0 +1,379 @@
+// lg_eig2.cu -- FP64 eigensolve + transform for the analysis path, organised
+// around the FP64 pipe of GB300.
+//
+// The FP64 pipe of this GPU retires about one warp instruction per 17 cycles per
+// SM whatever the number of active lanes, so scalar FP64 code costs as much as
+// full-warp code.  The solve (letkf_core.F90:98-225 + the update of
+// letkf_compute.F90:501-552) is therefore split so that every FP64 instruction
+// carries 32 useful lanes:
+//
+//   tridiag_kernel  one warp per matrix: Householder reduction C = Q T Q^T
+//                   (tred2's reduction half, FP64), writes diag, off-diagonal and
+//                   the reflectors (u_i, h_i).
+//   ql_kernel       one LANE per matrix: implicit QL iteration with Wilkinson
+//                   shifts on (d, e) -> eigenvalues; each Givens rotation
+//                   (c, s, i) is appended to a per-matrix log instead of being
+//                   accumulated into an eigenvector matrix.
+//   vec_kernel      one LANE per (matrix, vector): for t and every state row x the
+//                   solve owns, y = Q^T x, then the logged rotations forward
+//                   (y <- Z^T y); for t: overline_w-coefficients t_j / lambda_j;
+//                   for rows: dot = sum_j y_j t_j / lambda_j  (= overline_w . x),
+//                   y <- f(lambda) y, the rotations backward (Z y), then Q y
+//                   = W x.  xa = axb + W x + dot, recentred, is written directly.
+//
+// W and V are never formed; the cost per matrix is the reduction (2k^3/3 FMA)
+// plus O(k^2) per vector.  A matrix whose QL needs more rotations than the log
+// holds is flagged and redone by eig_apply_kernel (lg_eig.cu).
+#include <float.h>
+
+#include "lg_device.cuh"
+#include "lg_internal.h"
+
+namespace lg {
+
+namespace e2 {
+__device__ inline size_t tri_stride(int n) { return (size_t)n * (n + 3); }  // D,E,H + U
+__device__ inline size_t uoff(int i) { return (size_t)i * (i - 1) / 2; }   // row i of U (i >= 1)
+}  // namespace e2
+
+// ---------------------------------------------------------------- tridiag
+// scratch layout per solve: D[n] | E[n] | H[n] | U[n(n-1)/2]
+__global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const double* Cin,
+                                                     double* tri) {
+  const int s = blockIdx.x;
+  if (s >= nsolves) return;
+  const int LD = n | 1;
+  const int lane = threadIdx.x;
+  extern __shared__ double sm[];
+  double* a = sm;          // n x LD
+  double* e = a + n * LD;  // n
+  const double* C = Cin + (size_t)s * n * n;
+  for (int idx = lane; idx < n * n; idx += 32) {
+    const int i = idx % n, j = idx / n;
+    a[i * LD + j] = C[idx];
+  }
+  double* out = tri + (size_t)s * e2::tri_stride(n);
+  double* D = out;
+  double* E = out + n;
+  double* H = out + 2 * n;
+  double* U = out + 3 * n;
+  __syncwarp();
+  auto wsum = [](double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+  };
+  for (int i = n - 1; i >= 1; --i) {
+    const int l = i - 1;
+    double h = 0.0, ei;
+    if (l > 0) {
+      double sc = 0.0;
+      for (int kk = lane; kk <= l; kk += 32) sc += fabs(a[i * LD + kk]);
+      const double scale = wsum(sc);
+      if (scale == 0.0) {
+        ei = a[i * LD + l];
+      } else {
+        double hh = 0.0;
+        for (int kk = lane; kk <= l; kk += 32) {
+          const double v = a[i * LD + kk] / scale;
+          a[i * LD + kk] = v;
+          hh += v * v;
+        }
+        h = wsum(hh);
+        __syncwarp();
+        const double f = a[i * LD + l];
+        const double gg = (f >= 0.0) ? -sqrt(h) : sqrt(h);
+        ei = scale * gg;
+        h -= f * gg;
+        __syncwarp();
+        if (lane == 0) a[i * LD + l] = f - gg;
+        __syncwarp();
+        // p = A u / h
+        double fs = 0.0;
+        for (int j = lane; j <= l; j += 32) {
+          double gj = 0.0;
+          for (int kk = 0; kk <= j; ++kk) gj += a[j * LD + kk] * a[i * LD + kk];
+          for (int kk = j + 1; kk <= l; ++kk) gj += a[kk * LD + j] * a[i * LD + kk];
+          e[j] = gj / h;
+          fs += e[j] * a[i * LD + j];
+        }
+        const double hh2 = wsum(fs) / (h + h);
+        for (int j = lane; j <= l; j += 32) e[j] = e[j] - hh2 * a[i * LD + j];
+        __syncwarp();
+        for (int j = 0; j <= l; ++j) {
+          const double fj = a[i * LD + j], gj = e[j];
+          for (int kk = lane; kk <= j; kk += 32) a[j * LD + kk] -= (fj * e[kk] + gj * a[i * LD + kk]);
+        }
+        __syncwarp();
+      }
+    } else {
+      ei = a[i * LD + l];
+    }
+    // reflector of step i: u = a[i][0..i-1] (scaled), h
+    for (int kk = lane; kk < i; kk += 32) U[e2::uoff(i) + kk] = a[i * LD + kk];
+    if (lane == 0) {
+      H[i] = h;
+      E[i] = ei;
+    }
+    __syncwarp();
+  }
+  for (int i = lane; i < n; i += 32) D[i] = a[i * LD + i];
+  if (lane == 0) {
+    H[0] = 0.0;
+    E[0] = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------- QL
+// lane-private arrays in shared memory are interleaved [index][lane]
+__global__ void __launch_bounds__(128) ql_kernel(int n, int nsolves, double shift,
+                                                 const double* tri, double* lam, double2* rot_cs,
+                                                 unsigned char* rot_i, int* rot_n, int rot_cap,
+                                                 int* overflow_list, int* overflow_n,
+                                                 int* eig_fail) {
+  const int warps = blockDim.x / 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int s = (blockIdx.x * warps + w) * 32 + lane;
+  extern __shared__ double sm[];
+  double* d = sm + (size_t)w * 64 * n;  // n x 32
+  double* e = d + (size_t)32 * n;       // n x 32
+#define DD(i) d[(i) * 32 + lane]
+#define EE(i) e[(i) * 32 + lane]
+  if (s >= nsolves) return;
+  const double* T = tri + (size_t)s * e2::tri_stride(n);
+  for (int i = 0; i < n; ++i) {
+    DD(i) = T[i];
+    EE(i) = (i + 1 < n) ? T[n + i + 1] : 0.0;  // e[i] = T(i, i+1)
+  }
+  double2* cs_log = rot_cs + (size_t)s * rot_cap;
+  unsigned char* i_log = rot_i + (size_t)s * rot_cap;
+  int nrot = 0;
+  bool fail = false, over = false;
+  for (int l = 0; l < n && !fail; ++l) {
+    int iter = 0;
+    while (true) {
+      int m;
+      for (m = l; m < n - 1; ++m) {
+        const double dd = fabs(DD(m)) + fabs(DD(m + 1));
+        if (fabs(EE(m)) <= DBL_EPSILON * dd) break;
+      }
+      if (m == l) break;
+      if (++iter > 60) {
+        fail = true;
+        break;
+      }
+      double g = (DD(l + 1) - DD(l)) / (2.0 * EE(l));
+      double r = sqrt(g * g + 1.0);
+      g = DD(m) - DD(l) + EE(l) / (g + (g >= 0.0 ? r : -r));
+      double sn = 1.0, cn = 1.0, p = 0.0;
+      int i;
+      bool early = false;
+      for (i = m - 1; i >= l; --i) {
+        const double f = sn * EE(i), b = cn * EE(i);
+        r = sqrt(f * f + g * g);
+        EE(i + 1) = r;
+        if (r == 0.0) {
+          DD(i + 1) -= p;
+          EE(m) = 0.0;
+          early = true;
+          break;
+        }
+        const double rinv = 1.0 / r;
+        sn = f * rinv;
+        cn = g * rinv;
+        g = DD(i + 1) - p;
+        r = (DD(i) - g) * sn + 2.0 * cn * b;
+        p = sn * r;
+        DD(i + 1) = g + p;
+        g = cn * r - b;
+        if (nrot < rot_cap) {
+          cs_log[nrot] = make_double2(cn, sn);
+          i_log[nrot] = (unsigned char)i;
+        } else {
+          over = true;
+        }
+        ++nrot;
+      }
+      if (early) continue;
+      DD(l) -= p;
+      EE(l) = g;
+      EE(m) = 0.0;
+    }
+  }
+  for (int i = 0; i < n; ++i) lam[(size_t)s * n + i] = DD(i) * 1.0 + shift;
+  rot_n[s] = over ? -1 : nrot;
+  if (fail) atomicAdd(eig_fail, 1);
+  if (over) overflow_list[atomicAdd(overflow_n, 1)] = s;
+#undef DD
+#undef EE
+}
+
+// ---------------------------------------------------------------- vectors + update
+// lanes: solve-slot q = lane / per, vector v = lane % per (v = 0: t, v >= 1: row v-1)
+__global__ void __launch_bounds__(128) vec_kernel(Geometry g, SolveBatch b, const double* tin,
+                                                  const double* tri, const double* lam,
+                                                  const double2* rot_cs,
+                                                  const unsigned char* rot_i, const int* rot_n,
+                                                  int rot_cap, const double* xb,
+                                                  const double* axb, double* xa, double* axa) {
+  const int n = g.ens;
+  const bool vertical = g.vert_dist > 0.0;
+  const int nvec_max = 1 + (vertical ? g.n_var : g.n);
+  const int per = nvec_max;
+  const int slots = 32 / per;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int warps = blockDim.x / 32;
+  const int q = lane / per, v = lane % per;
+  const int s = (blockIdx.x * warps + w) * slots + q;
+  extern __shared__ double sm[];
+  double* y = sm + (size_t)w * 32 * n;  // this warp's lane vectors, n x 32 interleaved
+  // per-slot t_j / lambda_j, shared by the row lanes of the slot
+  double* tslot = sm + (size_t)warps * 32 * n + (size_t)w * slots * n;
+#define YY(i) y[(i) * 32 + lane]
+  const bool active = (lane < slots * per) && (s < b.nsolves);
+  int r_state = -1;  // state row of this lane
+  size_t ci = 0;
+  int nrot = 0;
+  const double* T = nullptr;
+  const double* L = nullptr;
+  if (active) {
+    const int col = b.first_col + s / b.levels;
+    const int kk = s % b.levels + 1;
+    const int glat = col % g.num_lat + 1, glon = col / g.num_lat + 1;
+    ci = (size_t)(glat - 1 + g.halo) + (size_t)(g.num_lat + 2 * g.halo) * (size_t)(glon - 1 + g.halo);
+    if (v >= 1) {
+      if (vertical) {
+        const int var = v - 1;
+        if (g.var_lev[var] == 1) {
+          if (kk == g.nz) r_state = g.var_start[var];
+        } else {
+          r_state = g.var_start[var] + kk - 1;
+        }
+      } else {
+        r_state = v - 1;
+      }
+    }
+    nrot = rot_n[s];
+    T = tri + (size_t)s * e2::tri_stride(n);
+    L = lam + (size_t)s * n;
+  }
+  const bool work = active && nrot >= 0 && (v == 0 || r_state >= 0);
+  if (work) {
+    // load x
+    if (v == 0) {
+      for (int i = 0; i < n; ++i) YY(i) = tin[(size_t)s * n + i];
+    } else {
+      const double* xr = xb + (size_t)n * (r_state + (size_t)g.n * ci);
+      for (int i = 0; i < n; ++i) YY(i) = xr[i];
+    }
+    const double* H = T + 2 * n;
+    const double* U = T + 3 * n;
+    // y = Q^T x = P_1 ... P_{n-1} x  (P_{n-1} first)
+    for (int i = n - 1; i >= 1; --i) {
+      const double h = H[i];
+      if (h == 0.0) continue;
+      const double* u = U + e2::uoff(i);
+      double dot = 0.0;
+      for (int kk = 0; kk < i; ++kk) dot += u[kk] * YY(kk);
+      dot /= h;
+      for (int kk = 0; kk < i; ++kk) YY(kk) -= u[kk] * dot;
+    }
+    // y = Z^T y: rotations in generation order
+    const double2* cs = rot_cs + (size_t)s * rot_cap;
+    const unsigned char* ix = rot_i + (size_t)s * rot_cap;
+    for (int r = 0; r < nrot; ++r) {
+      const double2 c = cs[r];
+      const int i = ix[r];
+      const double a0 = YY(i), a1 = YY(i + 1);
+      YY(i) = c.x * a0 - c.y * a1;
+      YY(i + 1) = c.y * a0 + c.x * a1;
+    }
+    if (v == 0) {
+      double* ts = tslot + (size_t)q * n;
+      for (int j = 0; j < n; ++j) ts[j] = YY(j) / L[j];
+    }
+  }
+  __syncwarp();
+  double dotw = 0.0;
+  if (work && v >= 1) {
+    const double* ts = tslot + (size_t)q * n;
+    const double km1 = (double)(n - 1);
+    for (int j = 0; j < n; ++j) {
+      dotw += YY(j) * ts[j];
+      YY(j) *= sqrt(km1 / L[j]);
+    }
+    // y = Z y: rotations in reverse order
+    const double2* cs = rot_cs + (size_t)s * rot_cap;
+    const unsigned char* ix = rot_i + (size_t)s * rot_cap;
+    for (int r = nrot - 1; r >= 0; --r) {
+      const double2 c = cs[r];
+      const int i = ix[r];
+      const double a0 = YY(i), a1 = YY(i + 1);
+      YY(i) = c.x * a0 + c.y * a1;
+      YY(i + 1) = -c.y * a0 + c.x * a1;
+    }
+    // y = Q y = P_{n-1} ... P_1 y  (P_1 first)
+    const double* H = T + 2 * n;
+    const double* U = T + 3 * n;
+    for (int i = 1; i < n; ++i) {
+      const double h = H[i];
+      if (h == 0.0) continue;
+      const double* u = U + e2::uoff(i);
+      double dot = 0.0;
+      for (int kk = 0; kk < i; ++kk) dot += u[kk] * YY(kk);
+      dot /= h;
+      for (int kk = 0; kk < i; ++kk) YY(kk) -= u[kk] * dot;
+    }
+    // xa = axb + W x + overline_w . x, recentred over members
+    const double ab = axb[r_state + (size_t)g.n * ci];
+    double mean = 0.0;
+    for (int ee = 0; ee < n; ++ee) mean += ab + (YY(ee) + dotw);
+    mean /= (double)n;
+    double* xo = xa + (size_t)n * (r_state + (size_t)g.n * ci);
+    for (int ee = 0; ee < n; ++ee) xo[ee] = (ab + (YY(ee) + dotw)) - mean;
+    axa[r_state + (size_t)g.n * ci] = mean;
+  }
+#undef YY
+}
+
+// ------------------------------------------------------------ host launchers
+size_t eig2_tri_doubles(int n) { return (size_t)n * (n + 3); }
+
+bool eig2_supported(const Geometry& g) {
+  const bool vertical = g.vert_dist > 0.0;
+  const int per = 1 + (vertical ? g.n_var : g.n);
+  return g.ens <= 128 && per <= 16;
+}
+
+void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
+                 const double* xb, const double* axb, double* xa, double* axa, double* tri,
+                 double* lam, double2* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
+                 int* overflow_list, int* overflow_n, int* eig_fail, cudaStream_t stream) {
+  const int n = g.ens;
+  const int ns = b.nsolves;
+  if (ns == 0) return;
+  // 1. tridiagonalisation
+  const size_t smem_t = sizeof(double) * ((size_t)n * (n | 1) + n);
+  cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t);
+  tridiag_kernel<<<ns, 32, smem_t, stream>>>(n, ns, C, tri);
+  // 2. QL, one solve per lane
+  const int ql_warps = 1;
+  const size_t smem_q = sizeof(double) * (size_t)ql_warps * 64 * n;
+  cudaFuncSetAttribute(ql_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_q);
+  const int ql_blocks = (ns + 32 * ql_warps - 1) / (32 * ql_warps);
+  ql_kernel<<<ql_blocks, 32 * ql_warps, smem_q, stream>>>(
+      n, ns, (double)(n - 1) / g.inflation, tri, lam, rot_cs, rot_i, rot_n, rot_cap, overflow_list,
+      overflow_n, eig_fail);
+  // 3. vectors and update
+  const bool vertical = g.vert_dist > 0.0;
+  const int per = 1 + (vertical ? g.n_var : g.n);
+  const int slots = 32 / per;
+  const int vwarps = 4;
+  const size_t smem_v = sizeof(double) * ((size_t)vwarps * 32 * n + (size_t)vwarps * slots * n);
+  cudaFuncSetAttribute(vec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_v);
+  const int vblocks = (ns + slots * vwarps - 1) / (slots * vwarps);
+  vec_kernel<<<vblocks, 32 * vwarps, smem_v, stream>>>(g, b, t, tri, lam, rot_cs, rot_i, rot_n,
+                                                       rot_cap, xb, axb, xa, axa);
+}
+
+}  // namespace lg

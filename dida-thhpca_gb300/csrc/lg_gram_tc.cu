@@ -1,0 +1,390 @@
+// lg_gram_tc.cu -- mixed-precision Gram matrix on the 5th-generation tensor cores.
+//
+// Same quantities as lg_gram.cu (letkf_core.F90:58-75,146-195), computed as one
+// BF16 x BF16 -> FP32 tcgen05.mma per 16 local entries:
+//
+//   y~_e = y_e * s_e  (s_e = sqrt(rdiaginv * rloc_k), FP32), split y~ = hi + lo (BF16)
+//   d~_e = s_e * d_e, split d~ = dhi + dlo
+//   A (M = 128 x K) = [ hi^T ; lo^T ]            rows 0..63 hi, 64..127 lo (members)
+//   B (K x N = 80)   = [ hi | dhi | dlo | 0 ]    columns 0..63 members, 64/65 innovation
+//   D = A B  (FP32 accumulator in tensor memory)
+//   C = D[0:64,0:64] + D[64:128,0:64] + D[64:128,0:64]^T     (hi hi + lo hi + hi lo)
+//   t = D[0:64,64] + D[0:64,65] + D[64:128,64]
+// The lo x lo and lo x dlo terms (relative 2^-16) are dropped.
+//
+// One CTA (4 warps) per solve.  Nonzero-weight entries are compacted into a
+// shared queue, 64 at a time they are scaled, split and written to one of two
+// shared-memory stages in the canonical K-major no-swizzle UMMA layout (8x16-byte
+// core matrices: LBO = 128 B between the two K halves of a 16-wide chunk,
+// SBO = 256 B between 8-row groups); thread 0 issues four MMAs per stage and
+// commits them to the stage's mbarrier, so the next stage's preparation
+// overlaps the tensor-core work.  Every mbarrier wait is bounded; on expiry the
+// kernel records LG_ERR_TIMEOUT, still waits (bounded) for its own MMAs, frees
+// its tensor memory and returns.
+#include <cuda_bf16.h>
+
+#include "lg_device.cuh"
+#include "lg_internal.h"
+
+namespace lg {
+
+namespace tc {
+
+constexpr int kThreads = 128;
+constexpr int kStageEntries = 64;           // 4 MMAs of K = 16
+constexpr int kChunkA = 128 * 16 * 2;       // 4096 B: M=128 x K=16 bf16
+constexpr int kChunkB = 80 * 16 * 2;        // 2560 B: N=80 x K=16 bf16
+constexpr int kStageBytes = 4 * (kChunkA + kChunkB);  // 26624 B
+constexpr int kN = 80;
+constexpr int kTmemCols = 128;
+constexpr int kQueueCap = kStageEntries + kThreads;
+constexpr long long kSpinLimit = 1ll << 24;  // ~1 s of polling
+
+__device__ inline uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// shared-memory matrix descriptor: K-major, no swizzle
+__device__ inline uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+  return d;                // base offset 0, layout type 0 (no swizzle)
+}
+
+// instruction descriptor: kind::f16, BF16 A/B, FP32 D, K-major A and B, M=128, N=80
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
+                            ((uint32_t)(128 >> 4) << 24);
+
+__device__ inline void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ inline bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait; returns false on expiry
+__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (long long i = 0; i < kSpinLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ inline void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ inline void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ inline void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ inline void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ inline void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 accumulator columns of this thread's lane
+__device__ inline void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ inline float schr2f(float ri) {
+  if (ri > 2.0f) return 0.0f;
+  if (ri > 1.0f) {
+    float rj = ri / 12.0f - 0.5f;
+    rj = rj * ri + 0.625f;
+    rj = rj * ri + 1.666667f;
+    return (rj * ri - 5.0f) * ri + 4.0f - 0.6666667f / ri;
+  }
+  if (ri > 0.0f) {
+    float rk = ri * ri;
+    float rj = (-0.25f * ri + 0.5f) * ri + 0.625f;
+    return (rj * ri - 1.666667f) * rk + 1.0f;
+  }
+  return 1.0f;
+}
+
+__device__ inline uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+}  // namespace tc
+
+__global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev hx, ListDev l,
+                                                              SolveBatch b, const double* axb,
+                                                              double* Cout, double* tout,
+                                                              int* err) {
+  using namespace tc;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* stage_base = smem_raw;  // 2 stages
+  __shared__ uint64_t mbar[2];
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int q_ent[kQueueCap];
+  __shared__ float q_s[kQueueCap];
+  __shared__ int q_n;
+  __shared__ float s_al;
+  __shared__ int s_fail;
+
+  const int s = blockIdx.x;
+  const int k = g.ens;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  int64_t base = 0;
+  int p = 0;
+  bool vertical = false;
+  if (b.mode == 0) {
+    const int col = b.first_col + s / b.levels;
+    const int kk = s % b.levels + 1;
+    base = l.off[col];
+    p = l.cnt[col];
+    vertical = g.vert_dist > 0.0;
+    if (vertical && tid == 0) {
+      const int glat = col % g.num_lat + 1, glon = col / g.num_lat + 1;
+      const size_t ci = (size_t)(glat - 1 + g.halo) +
+                        (size_t)(g.num_lat + 2 * g.halo) * (size_t)(glon - 1 + g.halo);
+      const double aps = axb[g.ps_row + (size_t)g.n * ci];
+      auto lev = [&](int k1) {
+        if (g.vcoord == LG_VCOORD_SIGMA) return g.ca[k1 - 1] * (aps - g.ptop) + g.ptop;
+        return g.ca[k1 - 1] * (g.p0 - g.ptop) + g.cb[k1 - 1] * (aps - g.ptop) + g.ptop;
+      };
+      s_al = (float)log(0.5 * (lev(kk) + lev(kk + 1)));
+    }
+  } else {
+    base = b.b_off[s];
+    p = b.b_nobsl[s];
+  }
+  // zero both stages once (the padding rows of B stay zero), init barriers
+  for (int i = tid; i < 2 * kStageBytes / 16; i += kThreads)
+    reinterpret_cast<uint4*>(stage_base)[i] = make_uint4(0, 0, 0, 0);
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    q_n = 0;
+    s_fail = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_sh)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem_d = tmem_base_sh;
+  const float al = s_al;
+  const float inv_vd = vertical ? (float)(1.0 / g.vert_dist) : 0.0f;
+
+  int scan = 0;
+  int nproc = 0;
+  int stage = 0;      // stages issued
+  uint32_t phase[2] = {0u, 0u};
+  bool ok = true;
+  while (true) {
+    // compact nonzero-weight entries into the queue
+    while (true) {
+      __syncthreads();
+      const int qn0 = q_n;
+      __syncthreads();  // everyone has read q_n before the next atomics
+      if (qn0 >= kStageEntries || scan >= p) break;
+      const int i = scan + tid;
+      if (i < p) {
+        int ent;
+        float w;
+        if (b.mode == 0) {
+          ent = l.ent[base + i];
+          float rl = (float)l.rloc[base + i];
+          if (vertical) {
+            const float z = fabsf(al - (float)hx.lnp[ent]) * inv_vd;
+            rl *= g.gc_filter_vertical ? schr2f(z) : (z > 2.0f ? 0.0f : 1.0f);
+          }
+          w = hx.rdiag[ent] * rl;
+        } else {
+          ent = i;
+          w = b.b_rdiag[base + i] * (float)b.b_rloc[base + i];
+        }
+        if (w > 0.0f) {
+          const int slot = atomicAdd(&q_n, 1);
+          q_ent[slot] = ent;
+          q_s[slot] = sqrtf(w);
+        }
+      }
+      scan += kThreads;
+    }
+    const int qn = q_n;
+    if (qn == 0) break;
+    const int nt = qn < kStageEntries ? qn : kStageEntries;
+    nproc += nt;
+    const int buf = stage & 1;
+    if (stage >= 2) {  // the MMAs that read this buffer two stages ago must be done
+      if (!mbar_wait(&mbar[buf], phase[buf])) ok = false;
+      phase[buf] ^= 1u;
+    }
+    unsigned char* A = stage_base + buf * kStageBytes;
+    unsigned char* B = A + 4 * kChunkA;
+    // scale, split and store: thread -> member m, entry groups of 8
+    {
+      const int m = tid & 63, g0 = tid >> 6;
+      for (int gi = g0; gi < 8; gi += 2) {
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int jj = 0; jj < 8; jj += 2) {
+          float v[2];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const int e = gi * 8 + jj + u;
+            float x = 0.0f;
+            if (e < nt && m < k) {
+              const int ent = q_ent[e];
+              const float* y = (b.mode == 0) ? hx.yb32 + (size_t)ent * k : nullptr;
+              const float yv = (b.mode == 0) ? y[m] : (float)b.b_hx[(size_t)(base + ent) * k + m];
+              x = yv * q_s[e];
+            }
+            v[u] = x;
+          }
+          __nv_bfloat162 h2 = __floats2bfloat162_rn(v[0], v[1]);
+          const float2 hf = __bfloat1622float2(h2);
+          hi[jj / 2] = *reinterpret_cast<uint32_t*>(&h2);
+          lo[jj / 2] = pack_bf16(v[0] - hf.x, v[1] - hf.y);
+        }
+        const int chunk = gi >> 1, kc = gi & 1;
+        const int off_row = (m >> 3) * 256 + kc * 128 + (m & 7) * 16;
+        *reinterpret_cast<uint4*>(A + chunk * kChunkA + off_row) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        const int mlo = m + 64;
+        const int off_lo = (mlo >> 3) * 256 + kc * 128 + (mlo & 7) * 16;
+        *reinterpret_cast<uint4*>(A + chunk * kChunkA + off_lo) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+        *reinterpret_cast<uint4*>(B + chunk * kChunkB + off_row) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+      }
+      // innovation rows 64 (hi) and 65 (lo) of B
+      if (tid < 8) {
+        const int gi = tid;
+        float dv[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int e = gi * 8 + j;
+          float x = 0.0f;
+          if (e < nt) {
+            const int ent = q_ent[e];
+            const double d = (b.mode == 0) ? hx.dis[ent] : b.b_dep[base + ent];
+            x = (float)d * q_s[e];
+          }
+          dv[j] = x;
+        }
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+          __nv_bfloat162 h2 = __floats2bfloat162_rn(dv[j], dv[j + 1]);
+          const float2 hf = __bfloat1622float2(h2);
+          hi[j / 2] = *reinterpret_cast<uint32_t*>(&h2);
+          lo[j / 2] = pack_bf16(dv[j] - hf.x, dv[j + 1] - hf.y);
+        }
+        const int chunk = gi >> 1, kc = gi & 1;
+        const int r64 = 8 * 256 + kc * 128 + 0 * 16, r65 = 8 * 256 + kc * 128 + 1 * 16;
+        *reinterpret_cast<uint4*>(B + chunk * kChunkB + r64) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4*>(B + chunk * kChunkB + r65) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      }
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      fence_after();
+      const uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const uint64_t da = make_desc(a0 + c * kChunkA, 128, 256);
+        const uint64_t db = make_desc(b0 + c * kChunkB, 128, 256);
+        mma_bf16(tmem_d, da, db, (stage > 0 || c > 0) ? 1u : 0u);
+      }
+      mma_commit(&mbar[buf]);
+    }
+    ++stage;
+    // drop the consumed entries from the queue
+    const int rem = qn - nt;
+    int te = 0;
+    float ts = 0.0f;
+    if (tid < rem) {
+      te = q_ent[nt + tid];
+      ts = q_s[nt + tid];
+    }
+    __syncthreads();
+    if (tid < rem) {
+      q_ent[tid] = te;
+      q_s[tid] = ts;
+    }
+    if (tid == 0) q_n = rem;
+  }
+
+  double* C = Cout + (size_t)s * k * k;
+  double* t = tout + (size_t)s * k;
+  if (stage == 0) {
+    for (int i = tid; i < k * k; i += kThreads) C[i] = 0.0;
+    for (int i = tid; i < k; i += kThreads) t[i] = 0.0;
+  } else {
+    // wait for the last commit (it covers every earlier MMA of this thread)
+    const int last = (stage - 1) & 1;
+    if (!mbar_wait(&mbar[last], phase[last])) ok = false;
+    fence_after();
+    float* D = reinterpret_cast<float*>(stage_base);  // 128 x 80, reuses the stages
+    for (int c0 = 0; c0 < kN; c0 += 16) {
+      float v[16];
+      tmem_ld16(tmem_d + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) D[(warp * 32 + lane) * kN + c0 + i] = v[i];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < k * k; idx += kThreads) {
+      const int i = idx % k, j = idx / k;
+      C[idx] = (double)D[i * kN + j] + (double)D[(64 + i) * kN + j] + (double)D[(64 + j) * kN + i];
+    }
+    for (int i = tid; i < k; i += kThreads)
+      t[i] = (double)D[i * kN + 64] + (double)D[i * kN + 65] + (double)D[(64 + i) * kN + 64];
+  }
+  if (!ok && tid == 0) s_fail = 1;
+  fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d),
+                 "r"(kTmemCols));
+  if (s_fail && tid == 0) atomicExch(err, LG_ERR_TIMEOUT);
+  if (b.work && tid == 0) atomicAdd(b.work, (unsigned long long)nproc);
+}
+
+bool gram_tc_supported(int ens) { return ens <= 64; }
+
+void launch_gram_tc(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
+                    const double* axb, double* C, double* t, int* err, cudaStream_t stream) {
+  if (b.nsolves == 0) return;
+  const size_t smem = 2 * tc::kStageBytes + 1024;
+  cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  gram_tc_kernel<<<b.nsolves, tc::kThreads, smem, stream>>>(g, hx, l, b, axb, C, t, err);
+}
+
+}  // namespace lg

@@ -98,6 +98,9 @@ struct SolveBatch {
   const double* b_dep;
   const double* b_rloc;
   unsigned long long* work;  // optional: += nonzero-weight entries processed
+  // optional: process only the solves listed in solve_list[0 .. *solve_count)
+  const int* solve_list;
+  const int* solve_count;
 };
 
 // kernels (host launchers), all asynchronous on `stream`
@@ -113,9 +116,18 @@ void launch_scan_counts(const int* cnt, int64_t* off, int n, void* tmp, size_t t
 size_t scan_tmp_bytes(int n);
 void launch_gram64(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
                    const double* axb, double* C, double* t, cudaStream_t stream);
+bool gram_tc_supported(int ens);
+void launch_gram_tc(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
+                    const double* axb, double* C, double* t, int* err, cudaStream_t stream);
 void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
                       const double* xb, const double* axb, double* xa, double* axa,
                       double* trans, double* wbar, int* eig_fail, cudaStream_t stream);
+size_t eig2_tri_doubles(int n);
+bool eig2_supported(const Geometry& g);
+void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
+                 const double* xb, const double* axb, double* xa, double* axa, double* tri,
+                 double* lam, double2* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
+                 int* overflow_list, int* overflow_n, int* eig_fail, cudaStream_t stream);
 void launch_nan_check(const double* x, size_t n, int* err, cudaStream_t stream);
 
 }  // namespace lg

@@ -24,6 +24,8 @@ UNITS = {
     "lg_search.cu": ["-fmad=false"],
     "lg_gram.cu": [],
     "lg_eig.cu": [],
+    "lg_gram_tc.cu": [],
+    "lg_eig2.cu": [],
 }
 
 

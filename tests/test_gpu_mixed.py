@@ -1,0 +1,93 @@
+"""GPU tests of the mixed-precision path (BF16 hi/lo tensor-core contractions,
+FP64 eigensolve) against the FP64 oracle.
+
+Bar: relative RMS of the analysis increment (xa_full - xb_full) <= 1e-4 per
+variable, the tolerance the mixed path is specified to.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_INCREMENT = 1e-4
+
+
+def increment_rel_rms(cfg, w, got, ref):
+    h = cfg.halo
+    xa, axa = got
+    xa_o, axa_o = ref
+    bg = (w.xb + w.axb[..., None])[h:-h, h:-h]
+    inc_g = (xa + axa[..., None])[h:-h, h:-h] - bg
+    inc_o = (xa_o + axa_o[..., None])[h:-h, h:-h] - bg
+    out = {}
+    r0 = 0
+    for v, lv in zip(cfg.var_names, cfg.var_lev):
+        sl = slice(r0, r0 + lv)
+        d = inc_g[:, :, sl] - inc_o[:, :, sl]
+        out[v] = float(np.sqrt(np.mean(d ** 2)) / np.sqrt(np.mean(inc_o[:, :, sl] ** 2)))
+        r0 += lv
+    return out
+
+
+def test_core_batch_mixed_close_to_fp64():
+    import letkf_gb300 as lg
+    from oracle import oracle as orc
+    import ctypes as C
+    import torch
+
+    rng = np.random.default_rng(7)
+    for k, p in [(16, 0), (16, 5), (40, 300), (64, 2000)]:
+        hx = rng.standard_normal((p, k))
+        hx -= hx.mean(axis=1, keepdims=True)
+        rd = (1.0 / rng.uniform(0.5, 2.0, p) ** 2).astype(np.float32)
+        dep = rng.standard_normal(p)
+        rloc = rng.uniform(0.0, 1.0, p)
+        trans_o, wbar_o = orc.core(hx, rd, dep, rloc, 1.05)
+        dev = torch.device("cuda")
+        t = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)
+        d_hx, d_rd, d_dep, d_rl = t(hx), t(rd), t(dep), t(rloc)
+        d_n = torch.tensor([p], dtype=torch.int32, device=dev)
+        d_off = torch.tensor([0], dtype=torch.int64, device=dev)
+        d_tr = torch.zeros((k, k), dtype=torch.float64, device=dev)
+        d_wb = torch.zeros(k, dtype=torch.float64, device=dev)
+        L = lg.load_library()
+        ptr = lambda x: C.c_void_p(x.data_ptr())
+        st = L.lg_core_batch(k, 1, ptr(d_n), ptr(d_off), ptr(d_hx), ptr(d_rd), ptr(d_dep),
+                             ptr(d_rl), 1.05, lg.LG_PREC_MIXED, ptr(d_tr), ptr(d_wb), None)
+        assert st == 0
+        torch.cuda.synchronize()
+        tr, wb = d_tr.cpu().numpy(), d_wb.cpu().numpy()
+        # BF16 hi/lo products with FP32 accumulation: ~1e-5 relative on trans
+        rel = np.linalg.norm(tr - trans_o) / np.linalg.norm(trans_o)
+        assert rel < 5e-5, (k, p, rel)
+        if p:
+            relw = np.linalg.norm(wb - wbar_o) / np.linalg.norm(wbar_o)
+            assert relw < 1e-4, (k, p, relw)
+
+
+@pytest.mark.parametrize("name,over", [("small3d", {}), ("tiny3d", {"ens": 64})])
+def test_mixed_analysis_increment_within_1e4(name, over):
+    import letkf_gb300 as lg
+    import synth
+    from oracle import oracle as orc
+
+    cfg = lg.preset(name).replace(precision=lg.LG_PREC_MIXED, **over)
+    w = synth.make_workload(cfg)
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    xa = np.zeros_like(w.xb)
+    axa = np.zeros_like(w.axb)
+    ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+    o = orc.Oracle(cfg, w.obs)
+    o.hx(w.xb, w.axb)
+    xa_o = np.zeros_like(w.xb)
+    axa_o = np.zeros_like(w.axb)
+    o.analysis(w.xb, w.axb, xa_o, axa_o)
+    errs = increment_rel_rms(cfg, w, (xa, axa), (xa_o, axa_o))
+    assert max(errs.values()) <= TOL_INCREMENT, errs
+    # lists are computed exactly in both precisions
+    counts, ent, _ = ctx.lists()
+    e_o, _ = o.column_list(5)
+    off = np.concatenate([[0], np.cumsum(counts)])
+    assert np.array_equal(ent[off[5]:off[6]], e_o)
+    ctx.letkf_final()

@@ -125,3 +125,12 @@ def test_core_batch_matches_oracle_core():
         trans_o, wbar_o = orc.core(hx, rd, dep, rloc, 1.05)
         assert np.allclose(trans, trans_o, rtol=1e-11, atol=1e-11), (k, p)
         assert np.allclose(wbar, wbar_o, rtol=1e-11, atol=1e-11), (k, p)
+
+
+def test_rotation_log_overflow_falls_back_to_accumulating_solver(monkeypatch):
+    """With a 5-rotation log every QL overflows; those solves are redone by the
+    eigenvector-accumulating solver and the analysis must still match."""
+    monkeypatch.setenv("LETKF_GB300_ROT_CAP", "5")
+    cfg, w, ctx, o, got, ref = _run_both("tiny3d")
+    assert _rel_err(cfg, w, got, ref[:2]) < RTOL_ANALYSIS
+    ctx.letkf_final()

@@ -64,6 +64,13 @@ struct lg_ctx {
   unsigned char* d_rot_i = nullptr;
   int *d_rot_n = nullptr, *d_ovf_list = nullptr;
   int rot_cap = 0;
+  // ln p bucketed records for the mixed-precision Gram
+  int* d_rec_ent = nullptr;
+  float *d_rec_lnp = nullptr, *d_rec_w = nullptr;
+  int* d_boff = nullptr;
+  size_t rec_cap = 0;
+  float lnp_lo = 0.0f, lnp_inv_dz = 1.0f;
+  static constexpr int kLnpBuckets = 128;
   // status words: [0] err, [1] eig_fail
   int* d_status = nullptr;
   unsigned long long* d_band = nullptr;
@@ -542,6 +549,20 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
   }
   d.dcx = dcx; d.dsx = dsx; d.dyr = dyr; d.fcx = fcx; d.fsx = fsx; d.fyr = fyr;
   lg::launch_obs_trig(d, dcx, dsx, dyr, fcx, fsx, fyr, c->own_stream);
+  {
+    double lo = 1e300, hi = -1e300;
+    for (int64_t i = 0; i < ph_off[n]; ++i) {
+      const double v = o->ph[i];
+      if (v > 0.0) {
+        lo = std::min(lo, log(v));
+        hi = std::max(hi, log(v));
+      }
+    }
+    if (!(hi >= lo)) lo = hi = 0.0;
+    const double span = std::max(hi - lo, 1e-3) * (1.0 + 1e-6);
+    c->lnp_lo = (float)(lo - 1e-6 * span);
+    c->lnp_inv_dz = (float)(lg_ctx::kLnpBuckets / span);
+  }
   c->types = tt;
   c->geo.n_types = T;
   lg::set_type_table(tt, c->own_stream);
@@ -608,6 +629,30 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   lg::launch_search(geo, c->obs, c->lists, 1, nullptr, st);
   launches += 1;
   CK(cudaGetLastError());
+  const bool mixed_tc = g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k);
+  lg::RecDev rec{};
+  if (mixed_tc) {
+    if (c->rec_cap < c->list_cap || !c->d_boff) {
+      dfree(c->d_rec_ent); dfree(c->d_rec_lnp); dfree(c->d_rec_w); dfree(c->d_boff);
+      int r = LG_OK;
+      r |= dalloc(&c->d_rec_ent, c->list_cap);
+      r |= dalloc(&c->d_rec_lnp, c->list_cap);
+      r |= dalloc(&c->d_rec_w, c->list_cap);
+      r |= dalloc(&c->d_boff, (size_t)ncol * (lg_ctx::kLnpBuckets + 1));
+      if (r != LG_OK) { c->rec_cap = 0; return LG_ERR_NOMEM; }
+      c->rec_cap = c->list_cap;
+    }
+    lg::launch_records(ncol, c->lists, c->hx, c->lnp_lo, c->lnp_inv_dz, lg_ctx::kLnpBuckets,
+                       c->d_boff, c->d_rec_ent, c->d_rec_lnp, c->d_rec_w, st);
+    launches += 1;
+    rec.ent = c->d_rec_ent;
+    rec.lnp = c->d_rec_lnp;
+    rec.w = c->d_rec_w;
+    rec.boff = c->d_boff;
+    rec.nb = lg_ctx::kLnpBuckets;
+    rec.lo = c->lnp_lo;
+    rec.inv_dz = c->lnp_inv_dz;
+  }
   CK(cudaEventRecord(c->ev[2], st));
   // solves, in column chunks bounded by the Gram workspace
   const int levels = g.vert_dist > 0.0 ? g.nz : 1;
@@ -654,8 +699,8 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
     b.nsolves = b.ncols * levels;
     b.work = c->d_work;
     CK(cudaEventRecord(c->kev[3 * q], st));
-    if (g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k))
-      lg::launch_gram_tc(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, c->d_status, st);
+    if (mixed_tc)
+      lg::launch_gram_tc(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, c->d_status, st, &rec);
     else
       lg::launch_gram64(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, st);
     CK(cudaEventRecord(c->kev[3 * q + 1], st));
@@ -801,6 +846,7 @@ void lg_destroy(lg_ctx* c) {
   dfree(c->d_C); dfree(c->d_t); dfree(c->d_status); dfree(c->d_band);
   dfree(c->d_tri); dfree(c->d_lam); dfree(c->d_rot_cs); dfree(c->d_rot_i); dfree(c->d_rot_n);
   dfree(c->d_ovf_list);
+  dfree(c->d_rec_ent); dfree(c->d_rec_lnp); dfree(c->d_rec_w); dfree(c->d_boff);
   dfree(c->d_xb); dfree(c->d_axb); dfree(c->d_xa); dfree(c->d_axa);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);

@@ -140,7 +140,7 @@ __device__ inline uint32_t pack_bf16(float a, float b) {
 __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev hx, ListDev l,
                                                               SolveBatch b, const double* axb,
                                                               double* Cout, double* tout,
-                                                              int* err) {
+                                                              int* err, RecDev rec) {
   using namespace tc;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* stage_base = smem_raw;  // 2 stages
@@ -158,9 +158,11 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev
 
   int64_t base = 0;
   int p = 0;
+  int col = 0;
   bool vertical = false;
+  const bool use_rec = (b.mode == 0) && rec.ent != nullptr;
   if (b.mode == 0) {
-    const int col = b.first_col + s / b.levels;
+    col = b.first_col + s / b.levels;
     const int kk = s % b.levels + 1;
     base = l.off[col];
     p = l.cnt[col];
@@ -204,6 +206,17 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev
   const float inv_vd = vertical ? (float)(1.0 / g.vert_dist) : 0.0f;
 
   int scan = 0;
+  if (use_rec && vertical) {
+    // only the ln p buckets within 2 vert_dist of this level (one bucket of slack)
+    const float span = 2.0f * (float)g.vert_dist;
+    int b_lo = (int)floorf((al - span - rec.lo) * rec.inv_dz) - 1;
+    int b_hi = (int)floorf((al + span - rec.lo) * rec.inv_dz) + 1;
+    b_lo = b_lo < 0 ? 0 : (b_lo > rec.nb - 1 ? rec.nb - 1 : b_lo);
+    b_hi = b_hi < 0 ? 0 : (b_hi > rec.nb - 1 ? rec.nb - 1 : b_hi);
+    const int* bo = rec.boff + (size_t)col * (rec.nb + 1);
+    scan = bo[b_lo];
+    p = bo[b_hi + 1];
+  }
   int nproc = 0;
   int stage = 0;      // stages issued
   uint32_t phase[2] = {0u, 0u};
@@ -219,7 +232,14 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev
       if (i < p) {
         int ent;
         float w;
-        if (b.mode == 0) {
+        if (use_rec) {
+          ent = rec.ent[base + i];
+          w = rec.w[base + i];
+          if (vertical) {
+            const float z = fabsf(al - rec.lnp[base + i]) * inv_vd;
+            w *= g.gc_filter_vertical ? schr2f(z) : (z > 2.0f ? 0.0f : 1.0f);
+          }
+        } else if (b.mode == 0) {
           ent = l.ent[base + i];
           float rl = (float)l.rloc[base + i];
           if (vertical) {
@@ -380,11 +400,14 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev
 bool gram_tc_supported(int ens) { return ens <= 64; }
 
 void launch_gram_tc(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
-                    const double* axb, double* C, double* t, int* err, cudaStream_t stream) {
+                    const double* axb, double* C, double* t, int* err, cudaStream_t stream,
+                    const RecDev* rec) {
   if (b.nsolves == 0) return;
   const size_t smem = 2 * tc::kStageBytes + 1024;
+  RecDev r{};
+  if (rec) r = *rec;
   cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  gram_tc_kernel<<<b.nsolves, tc::kThreads, smem, stream>>>(g, hx, l, b, axb, C, t, err);
+  gram_tc_kernel<<<b.nsolves, tc::kThreads, smem, stream>>>(g, hx, l, b, axb, C, t, err, r);
 }
 
 }  // namespace lg

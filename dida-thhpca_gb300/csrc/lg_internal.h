@@ -83,6 +83,16 @@ struct ListDev {
   int* capped;       // columns (1 if truncated at max_obs)
 };
 
+// Per-column entry records grouped by ln p bucket (mixed-precision Gram input).
+struct RecDev {
+  const int* ent;     // list-sized
+  const float* lnp;   // list-sized
+  const float* w;     // list-sized: rdiaginv * rloc (FP32)
+  const int* boff;    // columns x (nb+1)
+  int nb;
+  float lo, inv_dz;
+};
+
 // A batch of LETKF solves: which list entries feed it and where results go.
 struct SolveBatch {
   int mode;          // 0 = analysis columns, 1 = explicit core batch
@@ -118,7 +128,10 @@ void launch_gram64(const Geometry& g, const HxDev& hx, const ListDev& l, const S
                    const double* axb, double* C, double* t, cudaStream_t stream);
 bool gram_tc_supported(int ens);
 void launch_gram_tc(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
-                    const double* axb, double* C, double* t, int* err, cudaStream_t stream);
+                    const double* axb, double* C, double* t, int* err, cudaStream_t stream,
+                    const RecDev* rec = nullptr);
+void launch_records(int ncol, const ListDev& l, const HxDev& hx, float lo, float inv_dz, int nb,
+                    int* boff, int* rec_ent, float* rec_lnp, float* rec_w, cudaStream_t stream);
 void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
                       const double* xb, const double* axb, double* xa, double* axa,
                       double* trans, double* wbar, int* eig_fail, cudaStream_t stream);

@@ -143,3 +143,83 @@ void launch_scan_counts(const int* cnt, int64_t* off, int n, void* tmp, size_t t
 }
 
 }  // namespace lg
+
+namespace lg {
+
+// Per-column entry records for the mixed-precision Gram, grouped by ln p bucket.
+//
+// For every column the list entries are copied, in a stable counting sort by
+// bucket(ln p) = floor((ln p - lo) / dz), into (entry, ln p, rdiaginv * rloc)
+// records; boff[col * (nb + 1) + b] is the first record of bucket b.  A level's
+// non-zero vertical weights (|ln p_k - ln p| <= 2 vert_dist) then lie in a
+// contiguous bucket range, so each solve scans only its window instead of the
+// whole list.  One warp per column; the ranking inside a bucket uses the lane
+// order, so the layout is deterministic.
+__global__ void __launch_bounds__(128) records_kernel(int ncol, ListDev l, HxDev hx, float lo,
+                                                      float inv_dz, int nb, int* boff, int* rec_ent,
+                                                      float* rec_lnp, float* rec_w) {
+  const int warps = blockDim.x / 32;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int col = blockIdx.x * warps + w;
+  extern __shared__ int cur_all[];
+  int* cur = cur_all + w * (nb + 1);
+  if (col >= ncol) return;
+  for (int b = lane; b <= nb; b += 32) cur[b] = 0;
+  __syncwarp();
+  const int64_t base = l.off[col];
+  const int p = l.cnt[col];
+  auto bucket = [&](int ent) {
+    int b = (int)floorf(((float)hx.lnp[ent] - lo) * inv_dz);
+    return b < 0 ? 0 : (b >= nb ? nb - 1 : b);
+  };
+  // histogram
+  for (int i0 = 0; i0 < p; i0 += 32) {
+    const int i = i0 + lane;
+    if (i < p) atomicAdd(&cur[bucket(l.ent[base + i]) + 1], 1);
+  }
+  __syncwarp();
+  // exclusive scan over buckets (one lane; nb is small)
+  if (lane == 0) {
+    int acc = 0;
+    for (int b = 0; b <= nb; ++b) {
+      acc += cur[b];
+      cur[b] = acc;  // cur[b] = first record of bucket b
+    }
+  }
+  __syncwarp();
+  for (int b = lane; b <= nb; b += 32) boff[(size_t)col * (nb + 1) + b] = cur[b];
+  __syncwarp();
+  // stable scatter
+  const unsigned lt = (1u << lane) - 1u;
+  for (int i0 = 0; i0 < p; i0 += 32) {
+    const int i = i0 + lane;
+    const bool ok = i < p;
+    int ent = 0, b = nb;  // nb: out-of-range marker for inactive lanes
+    if (ok) {
+      ent = l.ent[base + i];
+      b = bucket(ent);
+    }
+    const unsigned same = __match_any_sync(0xffffffffu, b);
+    const int rank = __popc(same & lt);
+    const int start = cur[b];
+    __syncwarp();
+    if (ok) {
+      const int64_t pos = base + start + rank;
+      rec_ent[pos] = ent;
+      rec_lnp[pos] = (float)hx.lnp[ent];
+      rec_w[pos] = hx.rdiag[ent] * (float)l.rloc[base + i];
+    }
+    if (ok && rank == 0) cur[b] = start + __popc(same);
+    __syncwarp();
+  }
+}
+
+void launch_records(int ncol, const ListDev& l, const HxDev& hx, float lo, float inv_dz, int nb,
+                    int* boff, int* rec_ent, float* rec_lnp, float* rec_w, cudaStream_t stream) {
+  const int warps = 4;
+  const size_t smem = sizeof(int) * warps * (nb + 1);
+  records_kernel<<<(ncol + warps - 1) / warps, 32 * warps, smem, stream>>>(
+      ncol, l, hx, lo, inv_dz, nb, boff, rec_ent, rec_lnp, rec_w);
+}
+
+}  // namespace lg

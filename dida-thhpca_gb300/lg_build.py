@@ -26,6 +26,7 @@ UNITS = {
     "lg_eig.cu": [],
     "lg_gram_tc.cu": [],
     "lg_eig2.cu": [],
+    "lg_noalloc.cu": [],
 }
 
 

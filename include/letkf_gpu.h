@@ -197,6 +197,23 @@ int lg_core_batch(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
                   const double* d_rloc, double inflation, int precision,
                   double* d_trans, double* d_wbar, void* stream);
 
+/* lg_core_batch for callers that cannot allocate device memory: no counterpart
+ * in the reference.  A step being captured into a CUDA graph, a host framework
+ * that owns the device heap through its own pool, or a latency-critical loop
+ * that must not be serialised by cudaMalloc/cudaFree cannot let the library
+ * allocate its working memory; this entry point keeps it (Gram matrices,
+ * projected innovations, status word) in one fixed static device array of
+ * 8 MiB instead, so it needs nbatch * (ens*ens + ens) + 8 <= 1048576 doubles
+ * (e.g. at most 252 solves of 64 members per call) and returns LG_ERR_SHAPE
+ * beyond that.  Same arguments and results as lg_core_batch.  The array's
+ * device address is looked up on the first call made on each device, so make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+int lg_core_batch_noalloc(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
+                          const double* d_hxens, const float* d_rdiaginv, const double* d_dep,
+                          const double* d_rloc, double inflation, int precision,
+                          double* d_trans, double* d_wbar, void* stream);
+
 /* Fortran drop-in for the external letkf_core (all arguments by reference, host
  * arrays), so a build of the reference links this instead of its own letkf_core.
  * pflag is accepted and ignored.  Errors are reported through *ierr when the

@@ -46,6 +46,8 @@ struct lg_ctx {
   lg::ObsDev obs{};
   std::vector<void*> obs_bufs;
   std::vector<int> h_copy_obs, h_copy_block, h_copy_eoff;
+  lg::CellIndex cells{};
+  bool have_cells = false;
   // H(x)
   lg::HxDev hx{};
   size_t hx_entries_cap = 0;
@@ -77,6 +79,8 @@ struct lg_ctx {
   // staging for host-array runs
   double *d_xb = nullptr, *d_axb = nullptr, *d_xa = nullptr, *d_axa = nullptr;
   size_t state_elems = 0;
+  double *d_xin = nullptr, *d_spb = nullptr, *d_spa = nullptr;  // run_da_parallel staging
+  size_t da_elems = 0;
   lg_stats stats{};
   cudaEvent_t ev[5] = {};
   std::vector<cudaEvent_t> kev;  // per-launch events of the solve phase
@@ -566,6 +570,80 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
   c->types = tt;
   c->geo.n_types = T;
   lg::set_type_table(tt, c->own_stream);
+  // cell index of every (block, type) segment for the selection
+  {
+    const double pi = 3.14159265358979323846;
+    const double th = 2.0 * g.local_dist / (double)6371.393f;  // radians
+    double cap_deg;
+    if (th >= pi) {
+      cap_deg = 180.0;
+    } else {
+      const double v = std::max(-1.0, cos(th) - 2e-5);       // prefilter band included
+      cap_deg = acos(v) * 180.0 / pi + 0.01;
+    }
+    const double cell_deg = std::min(5.0, std::max(0.25, (cap_deg) / 4.0));
+    lg::CellIndex& ci = c->cells;
+    ci.cell_deg = (float)cell_deg;
+    ci.inv_cell = (float)(1.0 / cell_deg);
+    ci.cap_deg = (float)cap_deg;
+    ci.nrows = (int)ceil(180.0 / cell_deg) + 1;
+    ci.ncols = (int)ceil(360.0 / cell_deg) + 1;
+    ci.exact_rloc = g.precision == LG_PREC_FP64;
+    const int nseg = nb * T;
+    std::vector<int4> box(nseg);
+    std::vector<int> cell_off(nseg + 1, 0), cell_start, perm(ncopies);
+    std::vector<int> rowc(ncopies), colc(ncopies);
+    int max_len = 0;
+    for (int sg = 0; sg < nseg; ++sg) {
+      const int j0 = bt_off[sg], j1 = bt_off[sg + 1];
+      max_len = std::max(max_len, j1 - j0);
+      int r0 = ci.nrows, r1 = -1, c0 = ci.ncols, c1 = -1;
+      for (int j = j0; j < j1; ++j) {
+        const int oo = c->h_copy_obs[j];
+        int r = (int)floorf(((float)o->lat[oo] + 90.0f) * ci.inv_cell);
+        int cc = (int)floorf((float)o->lon[oo] * ci.inv_cell);
+        r = std::min(std::max(r, 0), ci.nrows - 1);
+        cc = std::min(std::max(cc, 0), ci.ncols - 1);
+        rowc[j] = r;
+        colc[j] = cc;
+        r0 = std::min(r0, r); r1 = std::max(r1, r);
+        c0 = std::min(c0, cc); c1 = std::max(c1, cc);
+      }
+      if (j1 == j0) { r0 = 0; r1 = 0; c0 = 0; c1 = 0; }
+      const int nr = r1 - r0 + 1, ncl = c1 - c0 + 1;
+      box[sg] = int4{r0, nr, c0, ncl};
+      const size_t base = cell_start.size();
+      cell_off[sg] = (int)base;
+      cell_start.resize(base + (size_t)nr * ncl + 1, 0);
+      int* cs = cell_start.data() + base;
+      for (int j = j0; j < j1; ++j) cs[(rowc[j] - r0) * ncl + (colc[j] - c0) + 1]++;
+      for (int q = 0; q < nr * ncl; ++q) cs[q + 1] += cs[q];
+      std::vector<int> fillp(cs, cs + (size_t)nr * ncl);
+      for (int j = j0; j < j1; ++j) {  // stable: positions ascend within a cell
+        const int cell = (rowc[j] - r0) * ncl + (colc[j] - c0);
+        perm[j0 + fillp[cell]++] = j - j0;
+      }
+    }
+    cell_off[nseg] = (int)cell_start.size();
+    ci.bitmap_words = std::max(1, (max_len + 31) / 32);
+    const int4* d_box = nullptr;
+    const int *d_cell_off = nullptr, *d_cell_start = nullptr, *d_perm = nullptr;
+    int rr = LG_OK;
+    rr |= upload(c, box.data(), box.size(), &d_box);
+    rr |= upload(c, cell_off.data(), cell_off.size(), &d_cell_off);
+    rr |= upload(c, cell_start.data(), cell_start.size(), &d_cell_start);
+    rr |= upload(c, perm.data(), perm.size(), &d_perm);
+    if (rr != LG_OK) {
+      free_obs(c);
+      return LG_ERR_NOMEM;
+    }
+    ci.box = d_box;
+    ci.cell_off = d_cell_off;
+    ci.cell_start = d_cell_start;
+    ci.perm = d_perm;
+    // one warp's bitmap must fit in shared memory
+    c->have_cells = (size_t)ci.bitmap_words * 4 * 4 <= (size_t)200 * 1024;
+  }
   CK(cudaStreamSynchronize(c->own_stream));
   if (ensure_hx(c, (size_t)ent) != LG_OK) {
     free_obs(c);
@@ -609,7 +687,10 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   CK(cudaGetLastError());
   CK(cudaEventRecord(c->ev[1], st));
   // selection: count, scan, fill
-  lg::launch_search(geo, c->obs, c->lists, 0, c->d_band, st);
+  if (c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH"))
+    lg::launch_search_cells(geo, c->obs, c->cells, c->lists, 0, c->d_band, st);
+  else
+    lg::launch_search(geo, c->obs, c->lists, 0, c->d_band, st);
   lg::launch_scan_counts(c->lists.cnt, c->lists.off, ncol, c->d_scan_tmp, c->scan_tmp_bytes, st);
   launches += 3;  // count pass + the scan's init and scan kernels
   int64_t total = 0;
@@ -626,7 +707,10 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
     c->list_cap = cap;
   }
   c->list_total = total;
-  lg::launch_search(geo, c->obs, c->lists, 1, nullptr, st);
+  if (c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH"))
+    lg::launch_search_cells(geo, c->obs, c->cells, c->lists, 1, nullptr, st);
+  else
+    lg::launch_search(geo, c->obs, c->lists, 1, nullptr, st);
   launches += 1;
   CK(cudaGetLastError());
   const bool mixed_tc = g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k);
@@ -708,7 +792,7 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
       CK(cudaMemsetAsync(c->d_status + 2, 0, sizeof(int), st));
       lg::launch_eig2(geo, b, c->d_C, c->d_t, xb, axb, xa, axa, c->d_tri, c->d_lam, c->d_rot_cs,
                       c->d_rot_i, c->d_rot_n, c->rot_cap, c->d_ovf_list, c->d_status + 2,
-                      c->d_status + 1, st);
+                      c->d_status + 1, g.precision == LG_PREC_MIXED, st);
       // matrices whose rotation log overflowed: accumulate-eigenvector solver
       lg::SolveBatch fb = b;
       fb.solve_list = c->d_ovf_list;
@@ -793,6 +877,79 @@ int lg_run(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* x
   return LG_OK;
 }
 
+int lg_split_mean_device(lg_ctx* c, const double* d_xb_in, double* d_xb, double* d_axb,
+                         void* stream_v) {
+  if (!c || !d_xb_in || !d_xb || !d_axb) return LG_ERR_ARG;
+  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+  const lg_config& g = c->cfg;
+  const int64_t rows =
+      (int64_t)(g.num_lat + 2 * g.halo) * (g.num_lon + 2 * g.halo) * (int64_t)c->geo.n;
+  int h_err = 0;
+  CK(cudaMemsetAsync(c->d_status + 3, 0, sizeof(int), st));
+  lg::launch_split_mean(g.ens, rows, d_xb_in, d_xb, d_axb, c->d_status + 3, st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(&h_err, c->d_status + 3, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return h_err;
+}
+
+int lg_post_device(lg_ctx* c, double gamma1, double gamma2, double polar_lat, const double* d_xb,
+                   const double* d_axb, const double* d_xa, const double* d_axa,
+                   double* d_xa_out, double* d_spread_b, double* d_spread_a, void* stream_v) {
+  if (!c || !d_xb || !d_axb || !d_xa || !d_axa || !d_xa_out || !d_spread_b || !d_spread_a)
+    return LG_ERR_ARG;
+  if (!c->have_grid) return LG_ERR_STATE;
+  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+  const lg_config& g = c->cfg;
+  lg::launch_post(g.ens, c->geo.n, g.num_lat, g.num_lon, g.halo, gamma1, gamma2, polar_lat,
+                  c->d_glat, d_xb, d_axb, d_xa, d_axa, d_xa_out, d_spread_b, d_spread_a, st);
+  CK(cudaGetLastError());
+  return LG_OK;
+}
+
+int lg_run_da_parallel(lg_ctx* c, int ntimes, double gamma1, double gamma2, double polar_lat,
+                       const double* xb_in, double* xa_out, double* spread_b, double* spread_a) {
+  if (!c || !xb_in || !xa_out || !spread_b || !spread_a) return LG_ERR_ARG;
+  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
+  const lg_config& g = c->cfg;
+  const size_t cols = (size_t)(g.num_lat + 2 * g.halo) * (g.num_lon + 2 * g.halo);
+  const size_t n = c->geo.n, k = g.ens;
+  const size_t inner = (size_t)g.num_lat * g.num_lon * n;
+  if (c->state_elems < cols * n * k) {
+    dfree(c->d_xb); dfree(c->d_axb); dfree(c->d_xa); dfree(c->d_axa);
+    int r = LG_OK;
+    r |= dalloc(&c->d_xb, cols * n * k);
+    r |= dalloc(&c->d_xa, cols * n * k);
+    r |= dalloc(&c->d_axb, cols * n);
+    r |= dalloc(&c->d_axa, cols * n);
+    if (r != LG_OK) { c->state_elems = 0; return LG_ERR_NOMEM; }
+    c->state_elems = cols * n * k;
+  }
+  if (c->da_elems < cols * n * k) {
+    dfree(c->d_xin); dfree(c->d_spb); dfree(c->d_spa);
+    int r = LG_OK;
+    r |= dalloc(&c->d_xin, cols * n * k);
+    r |= dalloc(&c->d_spb, inner);
+    r |= dalloc(&c->d_spa, inner);
+    if (r != LG_OK) { c->da_elems = 0; return LG_ERR_NOMEM; }
+    c->da_elems = cols * n * k;
+  }
+  cudaStream_t st = c->own_stream;
+  CK(cudaMemcpyAsync(c->d_xin, xb_in, sizeof(double) * cols * n * k, cudaMemcpyHostToDevice, st));
+  int r = lg_split_mean_device(c, c->d_xin, c->d_xb, c->d_axb, st);
+  if (r != LG_OK) return r;
+  r = lg_run_device(c, ntimes, c->d_xb, c->d_axb, c->d_xa, c->d_axa, st);
+  if (r != LG_OK) return r;
+  r = lg_post_device(c, gamma1, gamma2, polar_lat, c->d_xb, c->d_axb, c->d_xa, c->d_axa,
+                     c->d_xin, c->d_spb, c->d_spa, st);
+  if (r != LG_OK) return r;
+  CK(cudaMemcpyAsync(xa_out, c->d_xin, sizeof(double) * cols * n * k, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(spread_b, c->d_spb, sizeof(double) * inner, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(spread_a, c->d_spa, sizeof(double) * inner, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return LG_OK;
+}
+
 int lg_get_stats(const lg_ctx* c, lg_stats* st) {
   if (!c || !st) return LG_ERR_ARG;
   *st = c->stats;
@@ -848,6 +1005,7 @@ void lg_destroy(lg_ctx* c) {
   dfree(c->d_ovf_list);
   dfree(c->d_rec_ent); dfree(c->d_rec_lnp); dfree(c->d_rec_w); dfree(c->d_boff);
   dfree(c->d_xb); dfree(c->d_axb); dfree(c->d_xa); dfree(c->d_axa);
+  dfree(c->d_xin); dfree(c->d_spb); dfree(c->d_spa);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : c->kev) cudaEventDestroy(e);

@@ -14,7 +14,9 @@
 //                   shifts on (d, e) -> eigenvalues; each Givens rotation
 //                   (c, s, i) is appended to a per-matrix log instead of being
 //                   accumulated into an eigenvector matrix.
-//   vec_kernel      one LANE per (matrix, vector): for t and every state row x the
+//   vec_kernel      one LANE per (matrix, vector), FP64 (FP64 path) or FP32 (mixed
+//                   path: the Xb.W contraction; eigenvalues, rotations and
+//                   reflectors are still FP64 results): for t and every state row x the
 //                   solve owns, y = Q^T x, then the logged rotations forward
 //                   (y <- Z^T y); for t: overline_w-coefficients t_j / lambda_j;
 //                   for rows: dot = sum_j y_j t_j / lambda_j  (= overline_w . x),
@@ -74,8 +76,9 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
         ei = a[i * LD + l];
       } else {
         double hh = 0.0;
+        const double inv_scale = 1.0 / scale;
         for (int kk = lane; kk <= l; kk += 32) {
-          const double v = a[i * LD + kk] / scale;
+          const double v = a[i * LD + kk] * inv_scale;
           a[i * LD + kk] = v;
           hh += v * v;
         }
@@ -89,20 +92,35 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
         if (lane == 0) a[i * LD + l] = f - gg;
         __syncwarp();
         // p = A u / h
+        const double inv_h = 1.0 / h;
         double fs = 0.0;
         for (int j = lane; j <= l; j += 32) {
           double gj = 0.0;
           for (int kk = 0; kk <= j; ++kk) gj += a[j * LD + kk] * a[i * LD + kk];
           for (int kk = j + 1; kk <= l; ++kk) gj += a[kk * LD + j] * a[i * LD + kk];
-          e[j] = gj / h;
+          e[j] = gj * inv_h;
           fs += e[j] * a[i * LD + j];
         }
-        const double hh2 = wsum(fs) / (h + h);
+        const double hh2 = wsum(fs) * (0.5 * inv_h);
         for (int j = lane; j <= l; j += 32) e[j] = e[j] - hh2 * a[i * LD + j];
         __syncwarp();
-        for (int j = 0; j <= l; ++j) {
-          const double fj = a[i * LD + j], gj = e[j];
-          for (int kk = lane; kk <= j; kk += 32) a[j * LD + kk] -= (fj * e[kk] + gj * a[i * LD + kk]);
+        // A -= u q^T + q u^T over the lower triangle, flattened so that every
+        // lane carries an element: t = j(j+1)/2 + kk, lane t, t+32, ...
+        {
+          const int tot = (l + 1) * (l + 2) / 2;
+          int j = 0, kk = lane;
+          while (kk > j) {  // position of t = lane
+            kk -= j + 1;
+            ++j;
+          }
+          for (int t = lane; t < tot; t += 32) {
+            a[j * LD + kk] -= (a[i * LD + j] * e[kk] + e[j] * a[i * LD + kk]);
+            kk += 32;
+            while (kk > j) {
+              kk -= j + 1;
+              ++j;
+            }
+          }
         }
         __syncwarp();
       }
@@ -126,8 +144,18 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
 
 // ---------------------------------------------------------------- QL
 // lane-private arrays in shared memory are interleaved [index][lane]
+template <typename LT>
+__device__ inline LT make_rot(double c, double s);
+template <>
+__device__ inline double2 make_rot<double2>(double c, double s) { return make_double2(c, s); }
+template <>
+__device__ inline float2 make_rot<float2>(double c, double s) { return make_float2((float)c, (float)s); }
+
+// LT: element type of the rotation log (double2 for the FP64 path, float2 when the
+// rotations are only replayed in FP32 by the mixed-precision vector kernel)
+template <typename LT>
 __global__ void __launch_bounds__(128) ql_kernel(int n, int nsolves, double shift,
-                                                 const double* tri, double* lam, double2* rot_cs,
+                                                 const double* tri, double* lam, LT* rot_cs,
                                                  unsigned char* rot_i, int* rot_n, int rot_cap,
                                                  int* overflow_list, int* overflow_n,
                                                  int* eig_fail) {
@@ -145,7 +173,7 @@ __global__ void __launch_bounds__(128) ql_kernel(int n, int nsolves, double shif
     DD(i) = T[i];
     EE(i) = (i + 1 < n) ? T[n + i + 1] : 0.0;  // e[i] = T(i, i+1)
   }
-  double2* cs_log = rot_cs + (size_t)s * rot_cap;
+  LT* cs_log = rot_cs + (size_t)s * rot_cap;
   unsigned char* i_log = rot_i + (size_t)s * rot_cap;
   int nrot = 0;
   bool fail = false, over = false;
@@ -187,7 +215,7 @@ __global__ void __launch_bounds__(128) ql_kernel(int n, int nsolves, double shif
         DD(i + 1) = g + p;
         g = cn * r - b;
         if (nrot < rot_cap) {
-          cs_log[nrot] = make_double2(cn, sn);
+          cs_log[nrot] = make_rot<LT>(cn, sn);
           i_log[nrot] = (unsigned char)i;
         } else {
           over = true;
@@ -210,9 +238,12 @@ __global__ void __launch_bounds__(128) ql_kernel(int n, int nsolves, double shif
 
 // ---------------------------------------------------------------- vectors + update
 // lanes: solve-slot q = lane / per, vector v = lane % per (v = 0: t, v >= 1: row v-1)
+// VT: arithmetic of the vector transforms (double: FP64 path; float: the mixed
+// path's Xb.W contraction, with eigenvalues, rotations and reflectors from FP64)
+template <typename VT, typename LT>
 __global__ void __launch_bounds__(128) vec_kernel(Geometry g, SolveBatch b, const double* tin,
                                                   const double* tri, const double* lam,
-                                                  const double2* rot_cs,
+                                                  const LT* rot_cs,
                                                   const unsigned char* rot_i, const int* rot_n,
                                                   int rot_cap, const double* xb,
                                                   const double* axb, double* xa, double* axa) {
@@ -225,10 +256,11 @@ __global__ void __launch_bounds__(128) vec_kernel(Geometry g, SolveBatch b, cons
   const int warps = blockDim.x / 32;
   const int q = lane / per, v = lane % per;
   const int s = (blockIdx.x * warps + w) * slots + q;
-  extern __shared__ double sm[];
-  double* y = sm + (size_t)w * 32 * n;  // this warp's lane vectors, n x 32 interleaved
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  VT* sm = reinterpret_cast<VT*>(sm_raw);
+  VT* y = sm + (size_t)w * 32 * n;  // this warp's lane vectors, n x 32 interleaved
   // per-slot t_j / lambda_j, shared by the row lanes of the slot
-  double* tslot = sm + (size_t)warps * 32 * n + (size_t)w * slots * n;
+  VT* tslot = sm + (size_t)warps * 32 * n + (size_t)w * slots * n;
 #define YY(i) y[(i) * 32 + lane]
   const bool active = (lane < slots * per) && (s < b.nsolves);
   int r_state = -1;  // state row of this lane
@@ -261,10 +293,10 @@ __global__ void __launch_bounds__(128) vec_kernel(Geometry g, SolveBatch b, cons
   if (work) {
     // load x
     if (v == 0) {
-      for (int i = 0; i < n; ++i) YY(i) = tin[(size_t)s * n + i];
+      for (int i = 0; i < n; ++i) YY(i) = (VT)tin[(size_t)s * n + i];
     } else {
       const double* xr = xb + (size_t)n * (r_state + (size_t)g.n * ci);
-      for (int i = 0; i < n; ++i) YY(i) = xr[i];
+      for (int i = 0; i < n; ++i) YY(i) = (VT)xr[i];
     }
     const double* H = T + 2 * n;
     const double* U = T + 3 * n;
@@ -273,44 +305,48 @@ __global__ void __launch_bounds__(128) vec_kernel(Geometry g, SolveBatch b, cons
       const double h = H[i];
       if (h == 0.0) continue;
       const double* u = U + e2::uoff(i);
-      double dot = 0.0;
-      for (int kk = 0; kk < i; ++kk) dot += u[kk] * YY(kk);
-      dot /= h;
-      for (int kk = 0; kk < i; ++kk) YY(kk) -= u[kk] * dot;
+      VT dot = 0;
+      for (int kk = 0; kk < i; ++kk) dot += (VT)u[kk] * YY(kk);
+      dot /= (VT)h;
+      for (int kk = 0; kk < i; ++kk) YY(kk) -= (VT)u[kk] * dot;
     }
     // y = Z^T y: rotations in generation order
-    const double2* cs = rot_cs + (size_t)s * rot_cap;
+    const LT* cs = rot_cs + (size_t)s * rot_cap;
     const unsigned char* ix = rot_i + (size_t)s * rot_cap;
     for (int r = 0; r < nrot; ++r) {
-      const double2 c = cs[r];
+      const LT c = cs[r];
       const int i = ix[r];
-      const double a0 = YY(i), a1 = YY(i + 1);
-      YY(i) = c.x * a0 - c.y * a1;
-      YY(i + 1) = c.y * a0 + c.x * a1;
+      const VT a0 = YY(i), a1 = YY(i + 1);
+      YY(i) = (VT)c.x * a0 - (VT)c.y * a1;
+      YY(i + 1) = (VT)c.y * a0 + (VT)c.x * a1;
     }
     if (v == 0) {
-      double* ts = tslot + (size_t)q * n;
-      for (int j = 0; j < n; ++j) ts[j] = YY(j) / L[j];
+      VT* ts = tslot + (size_t)q * n;
+      for (int j = 0; j < n; ++j) ts[j] = (VT)((double)YY(j) / L[j]);
     }
   }
   __syncwarp();
-  double dotw = 0.0;
+  VT dotw = 0;
+  // W = sqrt(rho) I + V (f - sqrt(rho)) V^T with f_j = sqrt((k-1)/lambda_j): only
+  // the deviation, whose size is that of the analysis increment, goes through
+  // the VT-precision transforms; sqrt(rho) x is added in FP64 below.
+  const double srho = sqrt(g.inflation);
   if (work && v >= 1) {
-    const double* ts = tslot + (size_t)q * n;
+    const VT* ts = tslot + (size_t)q * n;
     const double km1 = (double)(n - 1);
     for (int j = 0; j < n; ++j) {
       dotw += YY(j) * ts[j];
-      YY(j) *= sqrt(km1 / L[j]);
+      YY(j) *= (VT)(sqrt(km1 / L[j]) - srho);
     }
     // y = Z y: rotations in reverse order
-    const double2* cs = rot_cs + (size_t)s * rot_cap;
+    const LT* cs = rot_cs + (size_t)s * rot_cap;
     const unsigned char* ix = rot_i + (size_t)s * rot_cap;
     for (int r = nrot - 1; r >= 0; --r) {
-      const double2 c = cs[r];
+      const LT c = cs[r];
       const int i = ix[r];
-      const double a0 = YY(i), a1 = YY(i + 1);
-      YY(i) = c.x * a0 + c.y * a1;
-      YY(i + 1) = -c.y * a0 + c.x * a1;
+      const VT a0 = YY(i), a1 = YY(i + 1);
+      YY(i) = (VT)c.x * a0 + (VT)c.y * a1;
+      YY(i + 1) = -(VT)c.y * a0 + (VT)c.x * a1;
     }
     // y = Q y = P_{n-1} ... P_1 y  (P_1 first)
     const double* H = T + 2 * n;
@@ -319,18 +355,21 @@ __global__ void __launch_bounds__(128) vec_kernel(Geometry g, SolveBatch b, cons
       const double h = H[i];
       if (h == 0.0) continue;
       const double* u = U + e2::uoff(i);
-      double dot = 0.0;
-      for (int kk = 0; kk < i; ++kk) dot += u[kk] * YY(kk);
-      dot /= h;
-      for (int kk = 0; kk < i; ++kk) YY(kk) -= u[kk] * dot;
+      VT dot = 0;
+      for (int kk = 0; kk < i; ++kk) dot += (VT)u[kk] * YY(kk);
+      dot /= (VT)h;
+      for (int kk = 0; kk < i; ++kk) YY(kk) -= (VT)u[kk] * dot;
     }
-    // xa = axb + W x + overline_w . x, recentred over members
+    // xa = axb + sqrt(rho) x + (W - sqrt(rho) I) x + overline_w . x, recentred
     const double ab = axb[r_state + (size_t)g.n * ci];
+    const double* xr = xb + (size_t)n * (r_state + (size_t)g.n * ci);
     double mean = 0.0;
-    for (int ee = 0; ee < n; ++ee) mean += ab + (YY(ee) + dotw);
+    for (int ee = 0; ee < n; ++ee)
+      mean += ab + (srho * xr[ee] + ((double)YY(ee) + (double)dotw));
     mean /= (double)n;
     double* xo = xa + (size_t)n * (r_state + (size_t)g.n * ci);
-    for (int ee = 0; ee < n; ++ee) xo[ee] = (ab + (YY(ee) + dotw)) - mean;
+    for (int ee = 0; ee < n; ++ee)
+      xo[ee] = (ab + (srho * xr[ee] + ((double)YY(ee) + (double)dotw))) - mean;
     axa[r_state + (size_t)g.n * ci] = mean;
   }
 #undef YY
@@ -345,10 +384,11 @@ bool eig2_supported(const Geometry& g) {
   return g.ens <= 128 && per <= 16;
 }
 
-void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
-                 const double* xb, const double* axb, double* xa, double* axa, double* tri,
-                 double* lam, double2* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
-                 int* overflow_list, int* overflow_n, int* eig_fail, cudaStream_t stream) {
+template <typename VT, typename LT>
+void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
+                   const double* xb, const double* axb, double* xa, double* axa, double* tri,
+                   double* lam, LT* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
+                   int* overflow_list, int* overflow_n, int* eig_fail, cudaStream_t stream) {
   const int n = g.ens;
   const int ns = b.nsolves;
   if (ns == 0) return;
@@ -359,9 +399,9 @@ void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const 
   // 2. QL, one solve per lane
   const int ql_warps = 1;
   const size_t smem_q = sizeof(double) * (size_t)ql_warps * 64 * n;
-  cudaFuncSetAttribute(ql_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_q);
+  cudaFuncSetAttribute(ql_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_q);
   const int ql_blocks = (ns + 32 * ql_warps - 1) / (32 * ql_warps);
-  ql_kernel<<<ql_blocks, 32 * ql_warps, smem_q, stream>>>(
+  ql_kernel<LT><<<ql_blocks, 32 * ql_warps, smem_q, stream>>>(
       n, ns, (double)(n - 1) / g.inflation, tri, lam, rot_cs, rot_i, rot_n, rot_cap, overflow_list,
       overflow_n, eig_fail);
   // 3. vectors and update
@@ -369,11 +409,27 @@ void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const 
   const int per = 1 + (vertical ? g.n_var : g.n);
   const int slots = 32 / per;
   const int vwarps = 4;
-  const size_t smem_v = sizeof(double) * ((size_t)vwarps * 32 * n + (size_t)vwarps * slots * n);
-  cudaFuncSetAttribute(vec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_v);
+  const size_t smem_v = sizeof(VT) * ((size_t)vwarps * 32 * n + (size_t)vwarps * slots * n);
+  cudaFuncSetAttribute(vec_kernel<VT, LT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_v);
   const int vblocks = (ns + slots * vwarps - 1) / (slots * vwarps);
-  vec_kernel<<<vblocks, 32 * vwarps, smem_v, stream>>>(g, b, t, tri, lam, rot_cs, rot_i, rot_n,
-                                                       rot_cap, xb, axb, xa, axa);
+  vec_kernel<VT, LT><<<vblocks, 32 * vwarps, smem_v, stream>>>(g, b, t, tri, lam, rot_cs, rot_i,
+                                                               rot_n, rot_cap, xb, axb, xa, axa);
+}
+
+void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
+                 const double* xb, const double* axb, double* xa, double* axa, double* tri,
+                 double* lam, void* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
+                 int* overflow_list, int* overflow_n, int* eig_fail, bool fp32_vectors,
+                 cudaStream_t stream) {
+  if (fp32_vectors)
+    launch_eig2_t<float, float2>(g, b, C, t, xb, axb, xa, axa, tri, lam,
+                                 static_cast<float2*>(rot_cs), rot_i, rot_n, rot_cap,
+                                 overflow_list, overflow_n, eig_fail, stream);
+  else
+    launch_eig2_t<double, double2>(g, b, C, t, xb, axb, xa, axa, tri, lam,
+                                   static_cast<double2*>(rot_cs), rot_i, rot_n, rot_cap,
+                                   overflow_list, overflow_n, eig_fail, stream);
 }
 
 }  // namespace lg

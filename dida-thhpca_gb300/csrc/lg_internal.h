@@ -65,6 +65,19 @@ struct ObsDev {
   const int* bt_off;     // nblocks*n_types+1: copies of (block, type)
 };
 
+// Cell index of each (block, type) segment of copies, for the selection.
+struct CellIndex {
+  int nrows, ncols;        // global cell grid
+  float cell_deg, inv_cell;
+  float cap_deg;           // search radius in degrees (2L/a with the prefilter margin)
+  int bitmap_words;        // max over segments of ceil(len/32)
+  int exact_rloc;          // 1: FP64 weights (FP64 path); 0: FP32 weights (mixed path)
+  const int4* box;         // per segment: row0, nrows, col0, ncols
+  const int* cell_off;     // per segment: offset of its cell_start block
+  const int* cell_start;   // per segment: nrows*ncols+1 offsets into perm
+  const int* perm;         // per copy slot: segment positions sorted by cell
+};
+
 // H(x) results per copy entry.
 struct HxDev {
   double* yb;     // n_entries * ens
@@ -121,6 +134,8 @@ void launch_hx(const Geometry& g, const ObsDev& o, const double* xb, const doubl
                HxDev hx, int* err, cudaStream_t stream);
 void launch_search(const Geometry& g, const ObsDev& o, ListDev l, int fill,
                    unsigned long long* band, cudaStream_t stream);
+void launch_search_cells(const Geometry& g, const ObsDev& o, const CellIndex& ci, ListDev l,
+                         int fill, unsigned long long* band, cudaStream_t stream);
 void launch_scan_counts(const int* cnt, int64_t* off, int n, void* tmp, size_t tmp_bytes,
                         cudaStream_t stream);
 size_t scan_tmp_bytes(int n);
@@ -139,8 +154,15 @@ size_t eig2_tri_doubles(int n);
 bool eig2_supported(const Geometry& g);
 void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
                  const double* xb, const double* axb, double* xa, double* axa, double* tri,
-                 double* lam, double2* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
-                 int* overflow_list, int* overflow_n, int* eig_fail, cudaStream_t stream);
+                 double* lam, void* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
+                 int* overflow_list, int* overflow_n, int* eig_fail, bool fp32_vectors,
+                 cudaStream_t stream);
+void launch_split_mean(int ens, int64_t npts_rows, const double* xb_in, double* xb, double* axb,
+                       int* err, cudaStream_t stream);
+void launch_post(int ens, int n, int num_lat, int num_lon, int halo, double gamma1, double gamma2,
+                 double polar, const float* glat, const double* xb, const double* axb,
+                 const double* xa, const double* axa, double* xa_out, double* spread_b,
+                 double* spread_a, cudaStream_t stream);
 void launch_nan_check(const double* x, size_t n, int* err, cudaStream_t stream);
 
 }  // namespace lg

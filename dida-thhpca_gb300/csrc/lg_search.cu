@@ -223,3 +223,211 @@ void launch_records(int ncol, const ListDev& l, const HxDev& hx, float lo, float
 }
 
 }  // namespace lg
+
+namespace lg {
+
+// Cell-indexed selection.  Same decisions and output order as search_kernel;
+// candidates come from the cells of each (block, type) segment that overlap
+// the column's spherical cap of radius 2L (plus a margin), instead of from the
+// whole segment.  The fill pass marks kept copies in a bitmap over the
+// segment's positions (observation-index order) and then emits them in that
+// order.
+__device__ inline bool keep_copy(const Geometry& g, const ObsDev& ob, int j, float fcx, float fsx,
+                                 float fyr, double ccx, double csx, double cyr,
+                                 const SearchArgs& sa, bool want_ri, double* ri_out,
+                                 unsigned long long* nband) {
+  const int o = ob.copy_obs[j];
+  if (!(fabs(ob.olat[o]) <= g.obs_polar)) return false;
+  const float v32 = ob.fcx[o] * fcx * cosf(ob.fyr[o] - fyr) + ob.fsx[o] * fsx;
+  const bool in_band = v32 <= sa.vhi && v32 >= sa.vlo;
+  double ri = 0.0;
+  if (in_band || (want_ri && v32 > sa.vhi)) {
+    const double dist = latlon_dist_pre(ob.dcx[o], ob.dsx[o], ob.dyr[o], ccx, csx, cyr);
+    ri = __ddiv_rn(__dmul_rn(dist, 1.0), g.local_dist);
+  }
+  bool keep;
+  if (in_band) {
+    keep = loc_fn(ri, g.gc_filter) > 0.0;
+    if (nband && fabs(ri - 2.0) < 1e-12) (*nband)++;
+  } else {
+    keep = v32 > sa.vhi;
+  }
+  if (ri_out) *ri_out = ri;
+  return keep;
+}
+
+__global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob, CellIndex ci,
+                                                           ListDev l, int fill, SearchArgs sa,
+                                                           unsigned long long* band) {
+  const int warps = blockDim.x / 32;
+  const int w = threadIdx.x >> 5;
+  const int col = blockIdx.x * warps + w;
+  const int ncol = g.num_lat * g.num_lon;
+  extern __shared__ unsigned int bitmap_all[];
+  unsigned int* bitmap = bitmap_all + (size_t)w * ci.bitmap_words;
+  if (col >= ncol) return;
+  const unsigned lane = threadIdx.x & 31u;
+  const int glat = col % g.num_lat + 1, glon = col / g.num_lat + 1;
+  const int b = g.lon_block[glon - 1] * g.global_nx + g.lat_block[glat - 1];
+  const double clat = (double)g.glat[glat - 1], clon = (double)g.glon[glon - 1];
+  const double ccx = cos(deg2rad_r8(clat)), csx = sin(deg2rad_r8(clat));
+  const double cyr = deg2rad_r8(clon);
+  const float pf = 3.14159274101257324f;
+  const float fcx = cosf((float)clat / 180.0f * pf), fsx = sinf((float)clat / 180.0f * pf);
+  const float fyr = (float)clon / 180.0f * pf;
+  // cap of angular radius theta (degrees) around the centre, in cell units
+  const float theta = ci.cap_deg;
+  const int r_lo = max(0, (int)floorf(((float)clat - theta + 90.0f) * ci.inv_cell));
+  const int r_hi = min(ci.nrows - 1, (int)floorf(((float)clat + theta + 90.0f) * ci.inv_cell));
+  float dlon = 180.0f;
+  if (fabsf((float)clat) + theta < 89.0f) {
+    const float sr = sinf(theta * (pf / 180.0f)) / cosf((float)clat * (pf / 180.0f));
+    if (sr < 1.0f) dlon = asinf(sr) * (180.0f / pf) * 1.001f + ci.cell_deg;
+  }
+  // longitude window [clon - dlon, clon + dlon] in degrees, split at 0/360 into
+  // at most two pieces of cell columns
+  const float w0 = (float)clon - dlon, w1 = (float)clon + dlon;
+  auto cidx = [&](float lon) {
+    const int c = (int)floorf(lon * ci.inv_cell);
+    return c < 0 ? 0 : (c > ci.ncols - 1 ? ci.ncols - 1 : c);
+  };
+  int pa0, pa1, pb0 = 1, pb1 = 0;
+  if (dlon >= 180.0f || w1 - w0 >= 360.0f) {
+    pa0 = 0;
+    pa1 = ci.ncols - 1;
+  } else if (w0 < 0.0f) {
+    pa0 = cidx(w0 + 360.0f); pa1 = ci.ncols - 1; pb0 = 0; pb1 = cidx(w1);
+  } else if (w1 >= 360.0f) {
+    pa0 = cidx(w0); pa1 = ci.ncols - 1; pb0 = 0; pb1 = cidx(w1 - 360.0f);
+  } else {
+    pa0 = cidx(w0); pa1 = cidx(w1);
+  }
+  const int T = g.n_types;
+  const int cap = g.max_obs > 0 ? g.max_obs : 0x7fffffff;
+  const bool exact_rloc = ci.exact_rloc;
+  int64_t written = 0;
+  const int64_t out0 = fill ? l.off[col] : 0;
+  unsigned long long nband = 0;
+  bool done = false;
+  for (int q = g.nb_off[b]; q < g.nb_off[b + 1] && !done; ++q) {
+    const int nbk = g.nb_blk[q];
+    for (int t = 0; t < T && !done; ++t) {
+      const int seg = nbk * T + t;
+      const int j0 = ob.bt_off[seg], len = ob.bt_off[seg + 1] - j0;
+      if (len == 0) continue;
+      const int nent = ob.copy_eoff[j0 + 1] - ob.copy_eoff[j0];  // same type in a segment
+      const int4 box = ci.box[seg];                                // row0, nrows, col0, ncols
+      const int* cs = ci.cell_start + ci.cell_off[seg];
+      const int* perm = ci.perm + j0;
+      if (fill)
+        for (int wd = lane; wd < (len + 31) / 32; wd += 32) bitmap[wd] = 0u;
+      __syncwarp();
+      int64_t seg_count = 0;
+      const int rr0 = max(r_lo, box.x), rr1 = min(r_hi, box.x + box.y - 1);
+      for (int r = rr0; r <= rr1; ++r) {
+        for (int piece = 0; piece < 2; ++piece) {
+          const int p0 = piece == 0 ? pa0 : pb0, p1 = piece == 0 ? pa1 : pb1;
+          const int cc0 = max(p0, box.z), cc1 = min(p1, box.z + box.w - 1);
+          if (cc0 > cc1) continue;
+          const int rowb = (r - box.x) * box.w;
+          const int i0 = cs[rowb + (cc0 - box.z)], i1 = cs[rowb + (cc1 - box.z) + 1];
+          for (int ib = i0; ib < i1; ib += 32) {
+            const int i = ib + (int)lane;
+            bool keep = false;
+            int pos = 0;
+            if (i < i1) {
+              pos = perm[i];
+              keep = keep_copy(g, ob, j0 + pos, fcx, fsx, fyr, ccx, csx, cyr, sa, false, nullptr,
+                               fill ? nullptr : &nband);
+            }
+            if (fill) {
+              if (keep) atomicOr(&bitmap[pos >> 5], 1u << (pos & 31));
+            } else {
+              seg_count += __popc(__ballot_sync(0xffffffffu, keep));
+            }
+          }
+        }
+      }
+      if (!fill) {
+        written += seg_count * nent;
+        if (written >= cap) done = true;
+        continue;
+      }
+      __syncwarp();
+      // emit the kept copies of this segment in position (observation-index) order
+      const int words = (len + 31) / 32;
+      for (int wb = 0; wb < words && !done; wb += 32) {
+        const int wd = wb + (int)lane;
+        const unsigned int bits = wd < words ? bitmap[wd] : 0u;
+        const int cnt = __popc(bits) * nent;
+        int incl = cnt;
+#pragma unroll
+        for (int sft = 1; sft < 32; sft <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, sft);
+          if ((int)lane >= sft) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int64_t posw = written + incl - cnt;
+        unsigned int rem = bits;
+        while (rem) {
+          const int bit = __ffs(rem) - 1;
+          rem &= rem - 1;
+          const int j = j0 + wd * 32 + bit;
+          const int o = ob.copy_obs[j];
+          double ri;
+          if (exact_rloc) {
+            const double dist = latlon_dist_pre(ob.dcx[o], ob.dsx[o], ob.dyr[o], ccx, csx, cyr);
+            ri = __ddiv_rn(__dmul_rn(dist, 1.0), g.local_dist);
+          } else {  // mixed path: the weight only needs FP32 accuracy
+            const float v32 = fminf(ob.fcx[o] * fcx * cosf(ob.fyr[o] - fyr) + ob.fsx[o] * fsx, 1.0f);
+            ri = (double)(6371.393f * acosf(v32) / (float)g.local_dist);
+          }
+          // a copy kept by the exact test has ri <= 2; clamp rounding beyond it
+          const double gc = loc_fn(fmin(ri, 2.0), g.gc_filter);
+          const int e0 = ob.copy_eoff[j];
+          for (int m = 0; m < nent; ++m, ++posw) {
+            if (posw < cap) {
+              l.ent[out0 + posw] = e0 + m;
+              l.rloc[out0 + posw] = gc;
+            }
+          }
+        }
+        written += total;
+        if (written >= cap) done = true;
+      }
+      __syncwarp();
+    }
+  }
+  if (!fill && lane == 0) {
+    l.cnt[col] = (int)(written < cap ? written : cap);
+    if (l.capped) l.capped[col] = written >= cap;
+  }
+  if (!fill && band) {
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) nband += __shfl_down_sync(0xffffffffu, nband, s);
+    if (lane == 0 && nband) atomicAdd(band, nband);
+  }
+}
+
+void launch_search_cells(const Geometry& g, const ObsDev& o, const CellIndex& ci, ListDev l,
+                         int fill, unsigned long long* band, cudaStream_t stream) {
+  const int ncol = g.num_lat * g.num_lon;
+  const double th = 2.0 * g.local_dist / earth_r4();
+  SearchArgs sa;
+  if (th >= 3.14159) {
+    sa.vlo = -3.0f;
+    sa.vhi = -2.0f;
+  } else {
+    const double v = cos(th);
+    sa.vlo = (float)(v - 1e-5);
+    sa.vhi = (float)(v + 1e-5);
+  }
+  const int warps = 4;
+  const size_t smem = sizeof(unsigned int) * (size_t)warps * ci.bitmap_words;
+  cudaFuncSetAttribute(search_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  search_cells_kernel<<<(ncol + warps - 1) / warps, 32 * warps, smem, stream>>>(g, o, ci, l, fill,
+                                                                                 sa, band);
+}
+
+}  // namespace lg

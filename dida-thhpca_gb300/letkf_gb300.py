@@ -174,6 +174,11 @@ def preset(name: str) -> Config:
     if name == "cfg5":
         return Config("cfg5", 128, 360, 720, 32, four, 500.0, 0.2, 1.03, 4_000_000, 16, 16,
                       obs_sigma=sig, max_obs=0, precision=LG_PREC_MIXED, clustered_frac=0.5)
+    # profiling case: cfg3's kernels at a quarter of the columns and observations
+    # (inputs above L2, a few GB on the device) for ncu captures
+    if name == "prof":
+        return Config("prof", 64, 90, 180, 32, four, 800.0, 0.2, 1.05, 250_000, 8, 8,
+                      obs_sigma=sig, max_obs=0, precision=LG_PREC_MIXED, sh_degree=20)
     # reduced cases for tests (seconds on the CPU oracle)
     if name == "tiny2d":
         return Config("tiny2d", 8, 18, 36, 1, ("x",), 1500.0, -1.0, 1.1, 300, 2, 3,
@@ -280,6 +285,12 @@ def load_library(path: str = LIB_PATH):
     lib.lg_letkf_core.argtypes = [C.c_int, C.c_int, P(C.c_double), P(C.c_float),
                                   P(C.c_double), P(C.c_double), P(C.c_double),
                                   P(C.c_double), C.c_double]
+    lib.lg_split_mean_device.argtypes = [C.c_void_p] * 4 + [C.c_void_p]
+    lib.lg_post_device.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double] + [C.c_void_p] * 8
+    lib.lg_run_da_parallel.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double,
+                                       P(C.c_double), P(C.c_double), P(C.c_double),
+                                       P(C.c_double)]
+    lib.lg_core_batch_noalloc.argtypes = lib.lg_core_batch.argtypes
     lib.lg_status_string.restype = C.c_char_p
     lib.lg_status_string.argtypes = [C.c_int]
     _lib = lib
@@ -369,6 +380,16 @@ class Letkf:
         check(self.lib.lg_run_device(self.h, ntimes, C.c_void_p(xb.data_ptr()),
                                      C.c_void_p(axb.data_ptr()), C.c_void_p(xa.data_ptr()),
                                      C.c_void_p(axa.data_ptr()), s), "lg_run_device")
+
+    def run_da_parallel(self, ntimes: int, gamma1: float, gamma2: float, polar_lat: float,
+                        xb_in: np.ndarray, xa_out: np.ndarray, spread_b: np.ndarray,
+                        spread_a: np.ndarray):
+        """run_da_parallel (module_da_parallel.F90:165-263) on host arrays: full
+        members in, blended members and spreads out."""
+        check(self.lib.lg_run_da_parallel(self.h, ntimes, gamma1, gamma2, polar_lat,
+                                          _ptr(xb_in, C.c_double), _ptr(xa_out, C.c_double),
+                                          _ptr(spread_b, C.c_double), _ptr(spread_a, C.c_double)),
+              "lg_run_da_parallel")
 
     def stats(self) -> dict:
         st = LgStats()

@@ -27,6 +27,7 @@ UNITS = {
     "lg_gram_tc.cu": [],
     "lg_eig2.cu": [],
     "lg_noalloc.cu": [],
+    "lg_prepost.cu": [],
 }
 
 

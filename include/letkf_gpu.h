@@ -164,6 +164,28 @@ int lg_run(lg_ctx* ctx, int ntimes, const double* xb, const double* axb, double*
 int lg_run_device(lg_ctx* ctx, int ntimes, const double* d_xb, const double* d_axb,
                   double* d_xa, double* d_axa, void* stream);
 
+/* The DA caller's pre-processing around letkf_run (run_da_parallel,
+ * x86/DA/EnDNN/src/module_da_parallel.F90:186-211), device arrays over the whole
+ * globe with halo: axb = sum(xb_in)/real(ens), xb = xb_in - axb.  Returns
+ * LG_ERR_NAN if any member value is NaN (the reference stops there). */
+int lg_split_mean_device(lg_ctx* ctx, const double* d_xb_in, double* d_xb, double* d_axb,
+                         void* stream);
+
+/* Its post-processing (module_da_parallel.F90:219-257): xa_out =
+ * gamma1*(axb+xb) + gamma2*(axa+xa) where |grid_lat| <= polar_lat, the
+ * background elsewhere, 0 in the halo; spread_b/spread_a (n, num_lat, num_lon),
+ * interior only, sqrt(sum of squares / ens). */
+int lg_post_device(lg_ctx* ctx, double gamma1, double gamma2, double polar_lat,
+                   const double* d_xb, const double* d_axb, const double* d_xa,
+                   const double* d_axa, double* d_xa_out, double* d_spread_b,
+                   double* d_spread_a, void* stream);
+
+/* run_da_parallel as a whole on host arrays (module_da_parallel.F90:165-263):
+ * split, letkf_run, blend and spreads.  xb_in/xa_out have the xb layout. */
+int lg_run_da_parallel(lg_ctx* ctx, int ntimes, double gamma1, double gamma2, double polar_lat,
+                       const double* xb_in, double* xa_out, double* spread_b,
+                       double* spread_a);
+
 /* Statistics of the last lg_run. */
 int lg_get_stats(const lg_ctx* ctx, lg_stats* st);
 

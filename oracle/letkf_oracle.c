@@ -995,3 +995,46 @@ int or_split_mean(int ens, int n, int64_t npts, const double* xb_in, double* xb,
     }
   return LG_OK;
 }
+
+/* run_da_parallel post-processing (module_da_parallel.F90:219-257) on whole-globe
+ * arrays with halo: RTPP blend gamma1*(axb+xb) + gamma2*(axa+xa) where
+ * |grid_lat(j)| <= polar, background elsewhere, zero in the halo; spreads
+ * (n, num_lat, num_lon) interior only. */
+int or_post(int ens, int n, int num_lat, int num_lon, int halo, const float* grid_lat,
+            double gamma1, double gamma2, double polar, const double* xb, const double* axb,
+            const double* xa, const double* axa, double* xa_out, double* spread_b,
+            double* spread_a) {
+  const int nlat_e = num_lat + 2 * halo, nlon_e = num_lon + 2 * halo;
+  for (int lo = 0; lo < nlon_e; ++lo)
+    for (int li = 0; li < nlat_e; ++li)
+      for (int k = 0; k < n; ++k) {
+        const size_t pr = (size_t)k + (size_t)n * ((size_t)li + (size_t)nlat_e * lo);
+        const int j = li - halo + 1, i = lo - halo + 1;
+        double* out = xa_out + pr * ens;
+        if (i < 1 || i > num_lon || j < 1 || j > num_lat) {
+          for (int e = 0; e < ens; ++e) out[e] = 0.0;
+          continue;
+        }
+        const double* b = xb + pr * ens;
+        const size_t s = (size_t)k + (size_t)n * ((size_t)(j - 1) + (size_t)num_lat * (i - 1));
+        double sb = 0.0, sa = 0.0;
+        if (fabs((double)grid_lat[j - 1]) <= polar) {
+          const double* x = xa + pr * ens;
+          for (int e = 0; e < ens; ++e)
+            out[e] = gamma1 * (axb[pr] + b[e]) + gamma2 * (axa[pr] + x[e]);
+          for (int e = 0; e < ens; ++e) {
+            sb = sb + b[e] * b[e];
+            sa = sa + (out[e] - axa[pr]) * (out[e] - axa[pr]);
+          }
+        } else {
+          for (int e = 0; e < ens; ++e) out[e] = b[e] + axb[pr];
+          for (int e = 0; e < ens; ++e) {
+            sb = sb + b[e] * b[e];
+            sa = sa + b[e] * b[e];
+          }
+        }
+        spread_b[s] = sqrt(sb / (double)(float)ens);
+        spread_a[s] = sqrt(sa / (double)(float)ens);
+      }
+  return LG_OK;
+}

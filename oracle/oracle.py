@@ -69,6 +69,8 @@ def lib(use_lapack: bool = True):
     L.or_schr.argtypes = [C.c_double]
     L.or_split_mean.argtypes = [C.c_int, C.c_int, C.c_int64, P(C.c_double), P(C.c_double),
                                 P(C.c_double)]
+    L.or_post.argtypes = [C.c_int] * 5 + [P(C.c_float), C.c_double, C.c_double, C.c_double] + [
+        P(C.c_double)] * 7
     if use_lapack:
         p = _openblas_path()
         if p:
@@ -172,3 +174,29 @@ def core(hxens, rdiaginv, dep, rloc, inflation):
     lib().or_core(k, p, _p(hx, C.c_double), _p(rd, C.c_float), _p(dp, C.c_double),
                   _p(rl, C.c_double), inflation, _p(trans, C.c_double), _p(wbar, C.c_double))
     return trans, wbar
+
+
+def split_mean(ens, xb_in):
+    """run_da_parallel pre-processing: (xb, axb) from full members (..., n, ens)."""
+    shp = xb_in.shape
+    n = shp[-2]
+    npts = int(np.prod(shp[:-2]))
+    xb = np.zeros_like(xb_in)
+    axb = np.zeros(shp[:-1])
+    r = lib().or_split_mean(ens, n, npts, _p(np.ascontiguousarray(xb_in), C.c_double),
+                            _p(xb, C.c_double), _p(axb, C.c_double))
+    return r, xb, axb
+
+
+def post(cfg, gamma1, gamma2, polar, xb, axb, xa, axa):
+    """run_da_parallel post-processing: xa_out and the two spreads."""
+    from letkf_gb300 import model_grid
+    lat, _ = model_grid(cfg)
+    xa_out = np.zeros_like(xb)
+    sb = np.zeros((cfg.num_lon, cfg.num_lat, xb.shape[-2]))
+    sa = np.zeros_like(sb)
+    lib().or_post(cfg.ens, xb.shape[-2], cfg.num_lat, cfg.num_lon, cfg.halo, _p(lat, C.c_float),
+                  gamma1, gamma2, polar, _p(xb, C.c_double), _p(axb, C.c_double),
+                  _p(xa, C.c_double), _p(axa, C.c_double), _p(xa_out, C.c_double),
+                  _p(sb, C.c_double), _p(sa, C.c_double))
+    return xa_out, sb, sa

@@ -134,3 +134,25 @@ def test_rotation_log_overflow_falls_back_to_accumulating_solver(monkeypatch):
     cfg, w, ctx, o, got, ref = _run_both("tiny3d")
     assert _rel_err(cfg, w, got, ref[:2]) < RTOL_ANALYSIS
     ctx.letkf_final()
+
+
+def test_linear_and_cell_indexed_selection_agree(monkeypatch):
+    """The cell-indexed selection and the plain scan of every neighbour-block
+    copy must produce identical lists."""
+    import letkf_gb300 as lg
+    import synth
+    cfg = lg.preset("small3d")
+    w = synth.make_workload(cfg)
+    out = []
+    for linear in (False, True):
+        if linear:
+            monkeypatch.setenv("LETKF_GB300_LINEAR_SEARCH", "1")
+        ctx = lg.Letkf(cfg)
+        ctx.set_obs(w.obs)
+        xa = np.zeros_like(w.xb)
+        axa = np.zeros_like(w.axb)
+        ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+        out.append(ctx.lists())
+        ctx.letkf_final()
+    (c0, e0, r0), (c1, e1, r1) = out
+    assert np.array_equal(c0, c1) and np.array_equal(e0, e1) and np.array_equal(r0, r1)

@@ -165,3 +165,27 @@ def test_boundary_observation_is_copied_into_both_blocks():
     o = oracle.Oracle(cfg, obs)
     co, cb, ce = o.copy_layout()
     assert (co == 0).sum() == 2
+
+
+def test_post_processing_kat():
+    """gamma1 = 0, gamma2 = 1 returns the analysis; poleward rows keep the
+    background; spreads are the RMS over members."""
+    import letkf_gb300 as lg
+    from oracle import oracle
+
+    cfg = lg.preset("tiny2d")
+    rng = np.random.default_rng(5)
+    shp = (cfg.num_lon + 2, cfg.num_lat + 2, 1, cfg.ens)
+    xb = rng.standard_normal(shp)
+    xa = rng.standard_normal(shp)
+    axb = rng.standard_normal(shp[:-1])
+    axa = rng.standard_normal(shp[:-1])
+    xo, sb, sa = oracle.post(cfg, 0.0, 1.0, 80.0, xb, axb, xa, axa)
+    lat, _ = lg.model_grid(cfg)
+    for j in range(cfg.num_lat):
+        if abs(lat[j]) <= 80.0:
+            assert np.allclose(xo[1:-1, j + 1], (axa[..., None] + xa)[1:-1, j + 1])
+        else:
+            assert np.allclose(xo[1:-1, j + 1], (axb[..., None] + xb)[1:-1, j + 1])
+    assert np.allclose(sb[:, :, 0], np.sqrt((xb[1:-1, 1:-1, 0] ** 2).mean(-1)))
+    assert (xo[0] == 0).all()

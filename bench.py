@@ -251,8 +251,8 @@ def main():
     sampler.start()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    acc = {"ms_gram": 0.0, "ms_eig": 0.0, "ms_hx": 0.0, "ms_search": 0.0, "n_launches": 0,
-           "n_gram_entries": 0}
+    acc = {"ms_gram": 0.0, "ms_eig": 0.0, "ms_hx": 0.0, "ms_search": 0.0, "ms_tridiag": 0.0,
+           "ms_ql": 0.0, "ms_vec": 0.0, "n_launches": 0, "n_gram_entries": 0, "n_chunks": 0}
     e0.record(stream)
     for _ in range(args.steps):
         step()
@@ -270,29 +270,40 @@ def main():
     value = world * ncol / (ms * 1e-3)
     st = ctx.stats()
 
-    # roofline of the dominant kernel (per-launch averages over the timed steps)
+    # roofline of the dominant kernel: algorithmic FLOPs of all its launches in
+    # the timed steps over the sum of their event-timed durations
     peaks = measured_peaks()
     k = cfg.ens
-    gram_flops = 2.0 * acc["n_gram_entries"] * k * k + 2.0 * acc["n_gram_entries"] * k
-    nchunk_launches = max(1, (acc["n_launches"] - 5 * args.steps) // 2)
     solves = st["n_solves"] * args.steps
-    eig_flops = solves * (4.0 * k ** 3 + 2.0 * k ** 3)  # tridiagonal+QL nominal 4k^3, sqrt 2k^3
     fp64_peak = fp64_peak_tflops(torch, dev)
+    mixed = cfg.precision == lg.LG_PREC_MIXED
     kernels = {
-        "gram": {"ms": acc["ms_gram"], "flops": gram_flops,
-                 "bound": "tensor" if cfg.precision == lg.LG_PREC_MIXED else "fp64"},
-        "eig_update": {"ms": acc["ms_eig"], "flops": eig_flops, "bound": "fp64"},
+        # 2 p k^2 (Gram, SURVEY convention) + 2 p k (Yb^T R^-1 d) over non-zero-weight entries
+        "gram": {"ms": acc["ms_gram"], "bound": "tensor" if mixed else "fp64",
+                 "flops": 2.0 * acc["n_gram_entries"] * k * k + 2.0 * acc["n_gram_entries"] * k},
+        # Householder tridiagonalisation of a symmetric k x k matrix: 4k^3/3
+        "tridiag": {"ms": acc["ms_tridiag"], "bound": "fp64", "flops": solves * 4.0 * k ** 3 / 3.0},
+        "ql": {"ms": acc["ms_ql"], "bound": "fp64", "flops": None},
+        "vec_update": {"ms": acc["ms_vec"], "bound": "fp32" if mixed else "fp64", "flops": None},
+        "search": {"ms": acc["ms_search"], "bound": "fp32/l2", "flops": None},
+        "hx": {"ms": acc["ms_hx"], "bound": "hbm", "flops": None},
     }
-    dom_name = max(kernels, key=lambda n: kernels[n]["ms"])
+    for name, kk in kernels.items():
+        kk["ms_per_step"] = kk["ms"] / args.steps
+        if kk["flops"] and kk["ms"] > 0:
+            kk["achieved_tflops"] = kk["flops"] / (kk["ms"] * 1e-3) / 1e12
+    dom_name = max((n for n in kernels if kernels[n]["flops"]), key=lambda n: kernels[n]["ms"])
     dom = kernels[dom_name]
     if dom["bound"] == "tensor":
         peak, peak_src = peaks.get("bf16_tflops", 1900.0), "bf16 burst, MEASURED_PEAKS.json"
     else:
-        peak, peak_src = fp64_peak, "cuBLAS DGEMM measured in this run"
-    achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12 if dom["ms"] > 0 else 0.0
+        peak, peak_src = fp64_peak, "cuBLAS DGEMM measured in this run (FP64 is not in MEASURED_PEAKS.json)"
+    achieved = dom.get("achieved_tflops", 0.0)
+    launches_dom = max(1, acc["n_chunks"])
     roofline = {"bound": dom["bound"], "kernel": dom_name, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
-                "peak_source": peak_src,
+                "peak_source": peak_src, "launches": launches_dom,
+                "ms_per_launch": dom["ms"] / launches_dom,
                 "share_of_step": dom["ms"] / (ms * args.steps)}
 
     line = {
@@ -311,8 +322,9 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clocks,
         "gpu_launches": acc["n_launches"],
-        "phases_ms": {"hx": acc["ms_hx"] / args.steps, "search": acc["ms_search"] / args.steps,
-                      "gram": acc["ms_gram"] / args.steps, "eig_update": acc["ms_eig"] / args.steps},
+        "phases_ms": {n: round(v["ms_per_step"], 3) for n, v in kernels.items()},
+        "kernels": {n: {kk: v[kk] for kk in ("bound", "achieved_tflops") if kk in v}
+                    for n, v in kernels.items()},
         "roofline": roofline,
         "fp64_peak_tflops": fp64_peak,
     }

@@ -85,6 +85,14 @@ struct lg_ctx {
   cudaEvent_t ev[5] = {};
   std::vector<cudaEvent_t> kev;  // per-launch events of the solve phase
   unsigned long long* d_work = nullptr;
+  // sizes fixed for the current observation set, and the captured analysis
+  bool capacity_ready = false;
+  int chunk = 1;
+  bool use_eig2 = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  const void* graph_key[5] = {};
+  int64_t graph_launches = 0;
+  bool graph_failed = false;
 };
 
 namespace {
@@ -228,6 +236,12 @@ double box_bound(float v) {
   char buf[64];
   snprintf(buf, sizeof buf, "%.5f", (double)v);
   return strtod(buf, nullptr);
+}
+
+void drop_graph(lg_ctx* c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  c->graph_exec = nullptr;
+  c->graph_key[0] = c->graph_key[1] = c->graph_key[2] = c->graph_key[3] = c->graph_key[4] = nullptr;
 }
 
 void free_obs(lg_ctx* c) {
@@ -451,6 +465,8 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
     }
   }
   free_obs(c);
+  c->capacity_ready = false;
+  drop_graph(c);
   const int n = o->n_obs, T = o->n_types;
   std::vector<int64_t> ph_off(n + 1, 0), val_off(n + 1, 0);
   for (int i = 0; i < n; ++i) {
@@ -653,19 +669,35 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
   return LG_OK;
 }
 
-int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* xa,
-                  double* axa, void* stream_v) {
-  (void)ntimes;
-  if (!c || !xb || !axb || !xa || !axa) return LG_ERR_ARG;
-  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
-  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+namespace {
+
+// Timing events of an analysis go through lg::record_event (lg_internal.h), which
+// keeps them valid inside a CUDA-graph capture.
+cudaError_t record_event(cudaEvent_t e, cudaStream_t st) { return lg::record_event(e, st); }
+
+// Milliseconds between two completed events; a failed query clears the error
+// it raised (it must not surface in a later, unrelated call) and reads as 0.
+float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    return 0.f;
+  }
+  return ms;
+}
+
+// Sizes every device buffer of the analysis for the current observation set:
+// the neighbour lists depend only on the grid and the observation positions,
+// so their total is known before any background arrives.  After this, an
+// analysis enqueues work only (no host synchronisation, no allocation), which
+// lets lg_run_device capture it into a CUDA graph.
+int prepare_capacity(lg_ctx* c) {
+  if (c->capacity_ready) return LG_OK;
   const lg_config& g = c->cfg;
   const Geometry& geo = c->geo;
   const int ncol = g.num_lat * g.num_lon;
   const int k = g.ens;
-  lg_stats& S = c->stats;
-  memset(&S, 0, sizeof S);
-  // list bookkeeping buffers
+  cudaStream_t st = c->own_stream;
   if (!c->lists.cnt) {
     int r = LG_OK;
     r |= dalloc(&c->lists.cnt, ncol + 1);
@@ -675,31 +707,20 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
     r |= dalloc((char**)&c->d_scan_tmp, c->scan_tmp_bytes);
     if (r != LG_OK) return LG_ERR_NOMEM;
   }
-  CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * 4, st));
-  CK(cudaMemsetAsync(c->d_band, 0, sizeof(unsigned long long), st));
-  CK(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), st));
-  int64_t launches = 0;
   CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
-  CK(cudaEventRecord(c->ev[0], st));
-  // H(x)
-  lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, st);
-  launches += c->obs.n_copies > 0;
-  CK(cudaGetLastError());
-  CK(cudaEventRecord(c->ev[1], st));
-  // selection: count, scan, fill
   if (c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH"))
-    lg::launch_search_cells(geo, c->obs, c->cells, c->lists, 0, c->d_band, st);
+    lg::launch_search_cells(geo, c->obs, c->cells, c->lists, 0, nullptr, st);
   else
-    lg::launch_search(geo, c->obs, c->lists, 0, c->d_band, st);
+    lg::launch_search(geo, c->obs, c->lists, 0, nullptr, st);
   lg::launch_scan_counts(c->lists.cnt, c->lists.off, ncol, c->d_scan_tmp, c->scan_tmp_bytes, st);
-  launches += 3;  // count pass + the scan's init and scan kernels
+  CK(cudaGetLastError());
   int64_t total = 0;
   CK(cudaMemcpyAsync(&total, c->lists.off + ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if ((size_t)total > c->list_cap || !c->lists.ent) {
     dfree(c->lists.ent);
     dfree(c->lists.rloc);
-    const size_t cap = (size_t)total + (size_t)total / 8 + 1024;
+    const size_t cap = (size_t)total + 1024;
     if (dalloc(&c->lists.ent, cap) != LG_OK || dalloc(&c->lists.rloc, cap) != LG_OK) {
       c->list_cap = 0;
       return LG_ERR_NOMEM;
@@ -707,53 +728,36 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
     c->list_cap = cap;
   }
   c->list_total = total;
-  if (c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH"))
-    lg::launch_search_cells(geo, c->obs, c->cells, c->lists, 1, nullptr, st);
-  else
-    lg::launch_search(geo, c->obs, c->lists, 1, nullptr, st);
-  launches += 1;
-  CK(cudaGetLastError());
   const bool mixed_tc = g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k);
-  lg::RecDev rec{};
-  if (mixed_tc) {
-    if (c->rec_cap < c->list_cap || !c->d_boff) {
-      dfree(c->d_rec_ent); dfree(c->d_rec_lnp); dfree(c->d_rec_w); dfree(c->d_boff);
-      int r = LG_OK;
-      r |= dalloc(&c->d_rec_ent, c->list_cap);
-      r |= dalloc(&c->d_rec_lnp, c->list_cap);
-      r |= dalloc(&c->d_rec_w, c->list_cap);
-      r |= dalloc(&c->d_boff, (size_t)ncol * (lg_ctx::kLnpBuckets + 1));
-      if (r != LG_OK) { c->rec_cap = 0; return LG_ERR_NOMEM; }
-      c->rec_cap = c->list_cap;
-    }
-    lg::launch_records(ncol, c->lists, c->hx, c->lnp_lo, c->lnp_inv_dz, lg_ctx::kLnpBuckets,
-                       c->d_boff, c->d_rec_ent, c->d_rec_lnp, c->d_rec_w, st);
-    launches += 1;
-    rec.ent = c->d_rec_ent;
-    rec.lnp = c->d_rec_lnp;
-    rec.w = c->d_rec_w;
-    rec.boff = c->d_boff;
-    rec.nb = lg_ctx::kLnpBuckets;
-    rec.lo = c->lnp_lo;
-    rec.inv_dz = c->lnp_inv_dz;
+  if (mixed_tc && (c->rec_cap < c->list_cap || !c->d_boff)) {
+    dfree(c->d_rec_ent); dfree(c->d_rec_lnp); dfree(c->d_rec_w); dfree(c->d_boff);
+    int r = LG_OK;
+    r |= dalloc(&c->d_rec_ent, c->list_cap);
+    r |= dalloc(&c->d_rec_lnp, c->list_cap);
+    r |= dalloc(&c->d_rec_w, c->list_cap);
+    r |= dalloc(&c->d_boff, (size_t)ncol * (lg_ctx::kLnpBuckets + 1));
+    if (r != LG_OK) { c->rec_cap = 0; return LG_ERR_NOMEM; }
+    c->rec_cap = c->list_cap;
   }
-  CK(cudaEventRecord(c->ev[2], st));
-  // solves, in column chunks bounded by the Gram workspace
+  // solve chunks bounded by the Gram workspace (1 GiB; LETKF_GB300_CHUNK_MB overrides
+  // it, e.g. to keep a profiler capture's device footprint small)
   const int levels = g.vert_dist > 0.0 ? g.nz : 1;
   const size_t per_col = (size_t)levels * k * k * sizeof(double);
-  int chunk = (int)std::min<size_t>((size_t)ncol, std::max<size_t>(1, ((size_t)1 << 30) / per_col));
-  const bool use_eig2 = lg::eig2_supported(geo);
-  if ((size_t)chunk * levels > c->solve_cap) {
+  size_t budget = (size_t)1 << 30;
+  if (const char* env = getenv("LETKF_GB300_CHUNK_MB")) budget = (size_t)std::max(1, atoi(env)) << 20;
+  c->chunk = (int)std::min<size_t>((size_t)ncol, std::max<size_t>(1, budget / per_col));
+  c->use_eig2 = lg::eig2_supported(geo);
+  if ((size_t)c->chunk * levels > c->solve_cap) {
     dfree(c->d_C); dfree(c->d_t); dfree(c->d_tri); dfree(c->d_lam); dfree(c->d_rot_cs);
     dfree(c->d_rot_i); dfree(c->d_rot_n); dfree(c->d_ovf_list);
-    const size_t cap = (size_t)chunk * levels;
+    const size_t cap = (size_t)c->chunk * levels;
     c->rot_cap = 3 * k * k;
     // test hook: a small log forces the overflow fallback path
     if (const char* env = getenv("LETKF_GB300_ROT_CAP")) c->rot_cap = std::max(1, atoi(env));
     int r = LG_OK;
     r |= dalloc(&c->d_C, cap * k * k);
     r |= dalloc(&c->d_t, cap * k);
-    if (use_eig2) {
+    if (c->use_eig2) {
       r |= dalloc(&c->d_tri, cap * lg::eig2_tri_doubles(k));
       r |= dalloc(&c->d_lam, cap * k);
       r |= dalloc(&c->d_rot_cs, cap * (size_t)c->rot_cap);
@@ -767,32 +771,86 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
     }
     c->solve_cap = cap;
   }
-  const int nchunks = (ncol + chunk - 1) / chunk;
-  while ((int)c->kev.size() < 3 * nchunks) {
+  const int nchunks = (ncol + c->chunk - 1) / c->chunk;
+  while ((int)c->kev.size() < 5 * nchunks) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
     c->kev.push_back(e);
   }
+  c->capacity_ready = true;
+  return LG_OK;
+}
+
+// Every kernel of one analysis, on stream st; no host synchronisation.
+int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, double* axa,
+                     cudaStream_t st, int64_t* launches_out) {
+  const lg_config& g = c->cfg;
+  const Geometry& geo = c->geo;
+  const int ncol = g.num_lat * g.num_lon;
+  const int k = g.ens;
+  int64_t launches = 0;
+  CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * 4, st));
+  CK(cudaMemsetAsync(c->d_band, 0, sizeof(unsigned long long), st));
+  CK(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), st));
+  CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
+  CK(record_event(c->ev[0], st));
+  // H(x)
+  lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, st);
+  launches += c->obs.n_copies > 0;
+  CK(record_event(c->ev[1], st));
+  // selection: count, scan, fill (the lists' capacity was sized by prepare_capacity)
+  const bool cells = c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH");
+  if (cells)
+    lg::launch_search_cells(geo, c->obs, c->cells, c->lists, 0, c->d_band, st);
+  else
+    lg::launch_search(geo, c->obs, c->lists, 0, c->d_band, st);
+  lg::launch_scan_counts(c->lists.cnt, c->lists.off, ncol, c->d_scan_tmp, c->scan_tmp_bytes, st);
+  launches += 3;  // count pass + the scan's init and scan kernels
+  if (cells)
+    lg::launch_search_cells(geo, c->obs, c->cells, c->lists, 1, nullptr, st);
+  else
+    lg::launch_search(geo, c->obs, c->lists, 1, nullptr, st);
+  launches += 1;
+  const bool mixed_tc = g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k);
+  lg::RecDev rec{};
+  if (mixed_tc) {
+    lg::launch_records(ncol, c->lists, c->hx, c->lnp_lo, c->lnp_inv_dz, lg_ctx::kLnpBuckets,
+                       c->d_boff, c->d_rec_ent, c->d_rec_lnp, c->d_rec_w, st);
+    launches += 1;
+    rec.ent = c->d_rec_ent;
+    rec.lnp = c->d_rec_lnp;
+    rec.w = c->d_rec_w;
+    rec.boff = c->d_boff;
+    rec.nb = lg_ctx::kLnpBuckets;
+    rec.lo = c->lnp_lo;
+    rec.inv_dz = c->lnp_inv_dz;
+  }
+  CK(record_event(c->ev[2], st));
+  const int levels = g.vert_dist > 0.0 ? g.nz : 1;
+  const int chunk = c->chunk;
+  const int nchunks = (ncol + chunk - 1) / chunk;
   for (int q = 0; q < nchunks; ++q) {
-    const int c0 = q * chunk;
     lg::SolveBatch b{};
     b.mode = 0;
-    b.first_col = c0;
-    b.ncols = std::min(chunk, ncol - c0);
+    b.first_col = q * chunk;
+    b.ncols = std::min(chunk, ncol - b.first_col);
     b.levels = levels;
     b.nsolves = b.ncols * levels;
     b.work = c->d_work;
-    CK(cudaEventRecord(c->kev[3 * q], st));
-    if (mixed_tc)
+    CK(record_event(c->kev[5 * q], st));
+    if (mixed_tc && !getenv("LETKF_GB300_GRAM_QUEUE"))
+      lg::launch_gram_tc_stream(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, c->d_status, rec, st);
+    else if (mixed_tc)
       lg::launch_gram_tc(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, c->d_status, st, &rec);
     else
       lg::launch_gram64(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, st);
-    CK(cudaEventRecord(c->kev[3 * q + 1], st));
-    if (use_eig2) {
-      CK(cudaMemsetAsync(c->d_status + 2, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(c->d_status + 2, 0, sizeof(int), st));
+    CK(record_event(c->kev[5 * q + 1], st));
+    if (c->use_eig2) {
       lg::launch_eig2(geo, b, c->d_C, c->d_t, xb, axb, xa, axa, c->d_tri, c->d_lam, c->d_rot_cs,
                       c->d_rot_i, c->d_rot_n, c->rot_cap, c->d_ovf_list, c->d_status + 2,
-                      c->d_status + 1, g.precision == LG_PREC_MIXED, st);
+                      c->d_status + 1, g.precision == LG_PREC_MIXED, st, c->kev[5 * q + 2],
+                      c->kev[5 * q + 3]);
       // matrices whose rotation log overflowed: accumulate-eigenvector solver
       lg::SolveBatch fb = b;
       fb.solve_list = c->d_ovf_list;
@@ -803,38 +861,99 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
     } else {
       lg::launch_eig_apply(geo, b, c->d_C, c->d_t, xb, axb, xa, axa, nullptr, nullptr,
                            c->d_status + 1, st);
+      CK(record_event(c->kev[5 * q + 2], st));
+      CK(record_event(c->kev[5 * q + 3], st));
       launches += 1;
     }
-    CK(cudaEventRecord(c->kev[3 * q + 2], st));
+    CK(record_event(c->kev[5 * q + 4], st));
     launches += 1;
   }
+  CK(record_event(c->ev[3], st));
   CK(cudaGetLastError());
-  CK(cudaEventRecord(c->ev[3], st));
+  *launches_out = launches;
+  return LG_OK;
+}
+
+}  // namespace
+
+int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* xa,
+                  double* axa, void* stream_v) {
+  (void)ntimes;
+  if (!c || !xb || !axb || !xa || !axa) return LG_ERR_ARG;
+  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
+  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+  const lg_config& g = c->cfg;
+  const int ncol = g.num_lat * g.num_lon;
+  lg_stats& S = c->stats;
+  memset(&S, 0, sizeof S);
+  int r = prepare_capacity(c);
+  if (r != LG_OK) return r;
+  int64_t launches = 0;
+  // The whole analysis is captured once into a CUDA graph per (arrays, stream)
+  // and replayed afterwards; LETKF_GB300_NO_GRAPH=1 runs it eagerly.
+  const bool graphs = !getenv("LETKF_GB300_NO_GRAPH") && !c->graph_failed;
+  const void* key[5] = {xb, axb, xa, axa, st};
+  bool ran = false;
+  if (graphs) {
+    if (c->graph_exec && memcmp(key, c->graph_key, sizeof key) != 0) drop_graph(c);
+    if (!c->graph_exec) {
+      cudaGraph_t graph = nullptr;
+      bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+      int er = LG_OK;
+      if (ok) er = enqueue_analysis(c, xb, axb, xa, axa, st, &launches);
+      const cudaError_t ee = ok ? cudaStreamEndCapture(st, &graph) : cudaErrorUnknown;
+      ok = ok && er == LG_OK && ee == cudaSuccess && graph != nullptr;
+      if (ok) ok = cudaGraphInstantiate(&c->graph_exec, graph, 0) == cudaSuccess;
+      if (graph) cudaGraphDestroy(graph);
+      if (!ok) {
+        cudaGetLastError();
+        c->graph_exec = nullptr;
+        c->graph_failed = true;  // keep running eagerly from now on
+      } else {
+        memcpy(c->graph_key, key, sizeof key);
+        c->graph_launches = launches;
+      }
+    }
+    if (c->graph_exec) {
+      CK(cudaGraphLaunch(c->graph_exec, st));
+      launches = c->graph_launches;
+      ran = true;
+    }
+  }
+  if (!ran) {
+    r = enqueue_analysis(c, xb, axb, xa, axa, st, &launches);
+    if (r != LG_OK) return r;
+  }
   int status[4];
   unsigned long long band = 0, work = 0;
   CK(cudaMemcpyAsync(status, c->d_status, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&band, c->d_band, sizeof(band), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&work, c->d_work, sizeof(work), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  const int nchunks = (ncol + c->chunk - 1) / c->chunk;
   for (int q = 0; q < nchunks; ++q) {
-    float a = 0.f, b2 = 0.f;
-    cudaEventElapsedTime(&a, c->kev[3 * q], c->kev[3 * q + 1]);
-    cudaEventElapsedTime(&b2, c->kev[3 * q + 1], c->kev[3 * q + 2]);
+    const float a = elapsed_ms(c->kev[5 * q], c->kev[5 * q + 1]);
+    const float t1 = elapsed_ms(c->kev[5 * q + 1], c->kev[5 * q + 2]);
+    const float t2 = elapsed_ms(c->kev[5 * q + 2], c->kev[5 * q + 3]);
+    const float t3 = elapsed_ms(c->kev[5 * q + 3], c->kev[5 * q + 4]);
     S.ms_gram += a;
-    S.ms_eig += b2;
+    S.ms_tridiag += t1;
+    S.ms_ql += t2;
+    S.ms_vec += t3;
+    S.ms_eig += t1 + t2 + t3;
   }
+  S.n_chunks = nchunks;
+  S.ms_hx = elapsed_ms(c->ev[0], c->ev[1]);
+  S.ms_search = elapsed_ms(c->ev[1], c->ev[2]);
+  S.ms_solve = elapsed_ms(c->ev[2], c->ev[3]);
+  S.ms_total = elapsed_ms(c->ev[0], c->ev[3]);
   S.n_launches = launches;
   S.n_gram_entries = (int64_t)work;
-  float ms;
-  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); S.ms_hx = ms;
-  cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); S.ms_search = ms;
-  cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); S.ms_solve = ms;
-  cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]); S.ms_total = ms;
   S.n_columns = ncol;
-  S.n_solves = (int64_t)ncol * levels;
+  S.n_solves = (int64_t)ncol * (g.vert_dist > 0.0 ? g.nz : 1);
   S.n_copies = c->obs.n_copies;
   S.n_entries = c->obs.n_entries;
-  S.nobsl_total = total;
+  S.nobsl_total = c->list_total;
   S.n_band = (int64_t)band;
   S.n_eig_fail = status[1];
   if (status[0] != 0) return status[0];
@@ -993,6 +1112,7 @@ int lg_get_hx(const lg_ctx* c, double* yb, double* dis) {
 
 void lg_destroy(lg_ctx* c) {
   if (!c) return;
+  drop_graph(c);
   free_obs(c);
   dfree(c->d_glat); dfree(c->d_glon); dfree(c->d_ca); dfree(c->d_cb); dfree(c->d_blk);
   dfree(c->d_lat_block); dfree(c->d_lon_block); dfree(c->d_nb_off); dfree(c->d_nb_blk);

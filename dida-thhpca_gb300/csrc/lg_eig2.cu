@@ -40,19 +40,44 @@ __device__ inline size_t uoff(int i) { return (size_t)i * (i - 1) / 2; }   // ro
 
 // ---------------------------------------------------------------- tridiag
 // scratch layout per solve: D[n] | E[n] | H[n] | U[n(n-1)/2]
+//
+// The matrix is held as its packed lower triangle, row j at j(j+1)/2 (16.6 KB for
+// 64 members, so 13 warps fit an SM).  Every shared-memory access pattern below
+// is free of bank conflicts within a half-warp: consecutive elements of a row,
+// the same column of consecutive rows j (offsets j(j+1)/2 + c, and j(j+1)/2 is a
+// permutation modulo 16 over any 16 consecutive j), or a broadcast.  The kernel
+// is bound by the FP64 pipe, so the instruction count is what is minimised: the
+// reflector needs no pre-scaling unless the row's squared norm leaves
+// [2^-900, 2^900], the matrix-vector product runs every lane over the same
+// number of terms (no divergent split at the diagonal), and the rank-2 update
+// is two fused multiply-adds per element.
+__device__ inline int tri_idx(int j) { return j * (j + 1) / 2; }
+
 __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const double* Cin,
                                                      double* tri) {
   const int s = blockIdx.x;
   if (s >= nsolves) return;
-  const int LD = n | 1;
   const int lane = threadIdx.x;
   extern __shared__ double sm[];
-  double* a = sm;          // n x LD
-  double* e = a + n * LD;  // n
+  const int np = n * (n + 1) / 2;
+  double* P = sm;      // packed lower triangle
+  double* q = P + np;  // n
   const double* C = Cin + (size_t)s * n * n;
-  for (int idx = lane; idx < n * n; idx += 32) {
-    const int i = idx % n, j = idx / n;
-    a[i * LD + j] = C[idx];
+  {
+    // element t of the packed triangle is (j, c) with t = j(j+1)/2 + c, c <= j
+    int j = 0, c = lane;
+    while (c > j) {
+      c -= j + 1;
+      ++j;
+    }
+    for (int t = lane; t < np; t += 32) {
+      P[t] = C[(size_t)j * n + c];
+      c += 32;
+      while (c > j) {
+        c -= j + 1;
+        ++j;
+      }
+    }
   }
   double* out = tri + (size_t)s * e2::tri_stride(n);
   double* D = out;
@@ -65,59 +90,74 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
   };
+  constexpr double kTiny = 0x1p-900, kHuge = 0x1p900;
   for (int i = n - 1; i >= 1; --i) {
     const int l = i - 1;
+    double* row = P + tri_idx(i);  // u: row i, columns 0..l
     double h = 0.0, ei;
     if (l > 0) {
-      double sc = 0.0;
-      for (int kk = lane; kk <= l; kk += 32) sc += fabs(a[i * LD + kk]);
-      const double scale = wsum(sc);
-      if (scale == 0.0) {
-        ei = a[i * LD + l];
-      } else {
-        double hh = 0.0;
-        const double inv_scale = 1.0 / scale;
-        for (int kk = lane; kk <= l; kk += 32) {
-          const double v = a[i * LD + kk] * inv_scale;
-          a[i * LD + kk] = v;
-          hh += v * v;
+      double ss = 0.0;
+      for (int c = lane; c <= l; c += 32) ss = fma(row[c], row[c], ss);
+      double h0 = wsum(ss);
+      double sc = 1.0;
+      if (!(h0 >= kTiny && h0 <= kHuge) && h0 != 0.0) {
+        // extreme magnitudes: scale the row by its 1-norm first (as tred2 does)
+        double a1 = 0.0;
+        for (int c = lane; c <= l; c += 32) a1 += fabs(row[c]);
+        sc = wsum(a1);
+        const double inv = 1.0 / sc;
+        ss = 0.0;
+        for (int c = lane; c <= l; c += 32) {
+          const double v = row[c] * inv;
+          row[c] = v;
+          ss = fma(v, v, ss);
         }
-        h = wsum(hh);
+        h0 = wsum(ss);
         __syncwarp();
-        const double f = a[i * LD + l];
-        const double gg = (f >= 0.0) ? -sqrt(h) : sqrt(h);
-        ei = scale * gg;
-        h -= f * gg;
+      }
+      if (h0 == 0.0) {
+        ei = row[l];
+      } else {
+        const double f = row[l];
+        const double gg = (f >= 0.0) ? -sqrt(h0) : sqrt(h0);
+        ei = sc * gg;
+        h = h0 - f * gg;
         __syncwarp();
-        if (lane == 0) a[i * LD + l] = f - gg;
+        if (lane == 0) row[l] = f - gg;
         __syncwarp();
-        // p = A u / h
+        // p = A u / h, lane j over row j: columns c <= j from row j, c > j from
+        // column j (the same trip count on every lane)
         const double inv_h = 1.0 / h;
         double fs = 0.0;
         for (int j = lane; j <= l; j += 32) {
+          const int tj = tri_idx(j);
           double gj = 0.0;
-          for (int kk = 0; kk <= j; ++kk) gj += a[j * LD + kk] * a[i * LD + kk];
-          for (int kk = j + 1; kk <= l; ++kk) gj += a[kk * LD + j] * a[i * LD + kk];
-          e[j] = gj * inv_h;
-          fs += e[j] * a[i * LD + j];
+          int tc = 0;  // c(c+1)/2
+          for (int c = 0; c <= l; ++c) {
+            const int off = (c <= j) ? tj + c : tc + j;
+            gj = fma(P[off], row[c], gj);
+            tc += c + 1;
+          }
+          const double pj = gj * inv_h;
+          q[j] = pj;
+          fs = fma(pj, row[j], fs);
         }
-        const double hh2 = wsum(fs) * (0.5 * inv_h);
-        for (int j = lane; j <= l; j += 32) e[j] = e[j] - hh2 * a[i * LD + j];
+        const double kq = wsum(fs) * (0.5 * inv_h);
+        for (int j = lane; j <= l; j += 32) q[j] = fma(-kq, row[j], q[j]);
         __syncwarp();
-        // A -= u q^T + q u^T over the lower triangle, flattened so that every
-        // lane carries an element: t = j(j+1)/2 + kk, lane t, t+32, ...
+        // A -= u q^T + q u^T over the packed rows 0..l, lane t, t+32, ...
         {
-          const int tot = (l + 1) * (l + 2) / 2;
-          int j = 0, kk = lane;
-          while (kk > j) {  // position of t = lane
-            kk -= j + 1;
+          const int tot = tri_idx(l + 1);
+          int j = 0, c = lane;
+          while (c > j) {
+            c -= j + 1;
             ++j;
           }
           for (int t = lane; t < tot; t += 32) {
-            a[j * LD + kk] -= (a[i * LD + j] * e[kk] + e[j] * a[i * LD + kk]);
-            kk += 32;
-            while (kk > j) {
-              kk -= j + 1;
+            P[t] = fma(-row[j], q[c], fma(-q[j], row[c], P[t]));
+            c += 32;
+            while (c > j) {
+              c -= j + 1;
               ++j;
             }
           }
@@ -125,17 +165,17 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
         __syncwarp();
       }
     } else {
-      ei = a[i * LD + l];
+      ei = row[l];
     }
-    // reflector of step i: u = a[i][0..i-1] (scaled), h
-    for (int kk = lane; kk < i; kk += 32) U[e2::uoff(i) + kk] = a[i * LD + kk];
+    // reflector of step i: u = row i (scaled), h
+    for (int c = lane; c < i; c += 32) U[e2::uoff(i) + c] = row[c];
     if (lane == 0) {
       H[i] = h;
       E[i] = ei;
     }
     __syncwarp();
   }
-  for (int i = lane; i < n; i += 32) D[i] = a[i * LD + i];
+  for (int i = lane; i < n; i += 32) D[i] = P[tri_idx(i) + i];
   if (lane == 0) {
     H[0] = 0.0;
     E[0] = 0.0;
@@ -167,46 +207,70 @@ __global__ void __launch_bounds__(128) ql_kernel(int n, int nsolves, double shif
   double* e = d + (size_t)32 * n;       // n x 32
 #define DD(i) d[(i) * 32 + lane]
 #define EE(i) e[(i) * 32 + lane]
-  if (s >= nsolves) return;
-  const double* T = tri + (size_t)s * e2::tri_stride(n);
-  for (int i = 0; i < n; ++i) {
-    DD(i) = T[i];
-    EE(i) = (i + 1 < n) ? T[n + i + 1] : 0.0;  // e[i] = T(i, i+1)
+  const bool live = s < nsolves;
+  if (live) {
+    const double* T = tri + (size_t)s * e2::tri_stride(n);
+    for (int i = 0; i < n; ++i) {
+      DD(i) = T[i];
+      EE(i) = (i + 1 < n) ? T[n + i + 1] : 0.0;  // e[i] = T(i, i+1)
+    }
   }
-  LT* cs_log = rot_cs + (size_t)s * rot_cap;
-  unsigned char* i_log = rot_i + (size_t)s * rot_cap;
-  int nrot = 0;
-  bool fail = false, over = false;
-  for (int l = 0; l < n && !fail; ++l) {
-    int iter = 0;
-    while (true) {
-      int m;
-      for (m = l; m < n - 1; ++m) {
-        const double dd = fabs(DD(m)) + fabs(DD(m + 1));
-        if (fabs(EE(m)) <= DBL_EPSILON * dd) break;
+  LT* cs_log = rot_cs + (size_t)(live ? s : 0) * rot_cap;
+  unsigned char* i_log = rot_i + (size_t)(live ? s : 0) * rot_cap;
+  // tql2's test |e_j| <= eps (|d_j| + |d_j+1|), with an integer pre-test on the
+  // biased exponents: a normal e_j with exponent >= max(exp d_j, exp d_j+1) - 49
+  // exceeds eps (|d_j| + |d_j+1|) < 2^-51 max(|d_j|, |d_j+1|), so the common
+  // "not negligible" answer costs no FP64 instruction.
+  auto bexp = [](double x) { return (__double2hiint(x) >> 20) & 0x7ff; };
+  auto negligible = [&](int j) {
+    const double ej = EE(j), a = DD(j), b = DD(j + 1);
+    const int ee = bexp(ej);
+    if (ee > 0 && ee + 49 >= max(bexp(a), bexp(b))) return false;
+    return fabs(ej) <= DBL_EPSILON * (fabs(a) + fabs(b));
+  };
+  // The lanes of a warp run their QL sweeps in step: one sweep per pass of the
+  // loop below, from the lane's first split m below l up to l, as in tql2.
+  int l = 0, iter = 0, nrot = 0;
+  bool fail = false, over = false, done = !live;
+  while (true) {
+    int m = n - 1;
+    if (!done) {
+      while (l < n - 1 && negligible(l)) {
+        ++l;
+        iter = 0;
       }
-      if (m == l) break;
-      if (++iter > 60) {
+      if (l >= n - 1) {
+        done = true;
+      } else if (++iter > 60) {
         fail = true;
-        break;
+        done = true;
+      } else {
+        for (m = l + 1; m < n - 1; ++m)
+          if (negligible(m)) break;
       }
+    }
+    if (__all_sync(0xffffffffu, done)) break;
+    if (!done) {
       double g = (DD(l + 1) - DD(l)) / (2.0 * EE(l));
       double r = sqrt(g * g + 1.0);
       g = DD(m) - DD(l) + EE(l) / (g + (g >= 0.0 ? r : -r));
       double sn = 1.0, cn = 1.0, p = 0.0;
-      int i;
       bool early = false;
-      for (i = m - 1; i >= l; --i) {
-        const double f = sn * EE(i), b = cn * EE(i);
-        r = sqrt(f * f + g * g);
-        EE(i + 1) = r;
-        if (r == 0.0) {
+      for (int i = m - 1; i >= l; --i) {
+        const double ei = EE(i);
+        const double f = sn * ei, b = cn * ei;
+        const double q2 = f * f + g * g;
+        if (q2 == 0.0) {
+          EE(i + 1) = 0.0;
           DD(i + 1) -= p;
           EE(m) = 0.0;
           early = true;
           break;
         }
-        const double rinv = 1.0 / r;
+        // one reciprocal square root gives both r and 1/r
+        const double rinv = rsqrt(q2);
+        r = q2 * rinv;
+        EE(i + 1) = r;
         sn = f * rinv;
         cn = g * rinv;
         g = DD(i + 1) - p;
@@ -222,12 +286,14 @@ __global__ void __launch_bounds__(128) ql_kernel(int n, int nsolves, double shif
         }
         ++nrot;
       }
-      if (early) continue;
-      DD(l) -= p;
-      EE(l) = g;
-      EE(m) = 0.0;
+      if (!early) {
+        DD(l) -= p;
+        EE(l) = g;
+        EE(m) = 0.0;
+      }
     }
   }
+  if (!live) return;
   for (int i = 0; i < n; ++i) lam[(size_t)s * n + i] = DD(i) * 1.0 + shift;
   rot_n[s] = over ? -1 : nrot;
   if (fail) atomicAdd(eig_fail, 1);
@@ -388,14 +454,16 @@ template <typename VT, typename LT>
 void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
                    const double* xb, const double* axb, double* xa, double* axa, double* tri,
                    double* lam, LT* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
-                   int* overflow_list, int* overflow_n, int* eig_fail, cudaStream_t stream) {
+                   int* overflow_list, int* overflow_n, int* eig_fail, cudaStream_t stream,
+                   cudaEvent_t ev_tri, cudaEvent_t ev_ql) {
   const int n = g.ens;
   const int ns = b.nsolves;
   if (ns == 0) return;
   // 1. tridiagonalisation
-  const size_t smem_t = sizeof(double) * ((size_t)n * (n | 1) + n);
+  const size_t smem_t = sizeof(double) * ((size_t)n * (n + 1) / 2 + n);
   cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t);
   tridiag_kernel<<<ns, 32, smem_t, stream>>>(n, ns, C, tri);
+  if (ev_tri) record_event(ev_tri, stream);
   // 2. QL, one solve per lane
   const int ql_warps = 1;
   const size_t smem_q = sizeof(double) * (size_t)ql_warps * 64 * n;
@@ -404,6 +472,7 @@ void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, cons
   ql_kernel<LT><<<ql_blocks, 32 * ql_warps, smem_q, stream>>>(
       n, ns, (double)(n - 1) / g.inflation, tri, lam, rot_cs, rot_i, rot_n, rot_cap, overflow_list,
       overflow_n, eig_fail);
+  if (ev_ql) record_event(ev_ql, stream);
   // 3. vectors and update
   const bool vertical = g.vert_dist > 0.0;
   const int per = 1 + (vertical ? g.n_var : g.n);
@@ -421,15 +490,15 @@ void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const 
                  const double* xb, const double* axb, double* xa, double* axa, double* tri,
                  double* lam, void* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
                  int* overflow_list, int* overflow_n, int* eig_fail, bool fp32_vectors,
-                 cudaStream_t stream) {
+                 cudaStream_t stream, cudaEvent_t ev_tri, cudaEvent_t ev_ql) {
   if (fp32_vectors)
     launch_eig2_t<float, float2>(g, b, C, t, xb, axb, xa, axa, tri, lam,
                                  static_cast<float2*>(rot_cs), rot_i, rot_n, rot_cap,
-                                 overflow_list, overflow_n, eig_fail, stream);
+                                 overflow_list, overflow_n, eig_fail, stream, ev_tri, ev_ql);
   else
     launch_eig2_t<double, double2>(g, b, C, t, xb, axb, xa, axa, tri, lam,
                                    static_cast<double2*>(rot_cs), rot_i, rot_n, rot_cap,
-                                   overflow_list, overflow_n, eig_fail, stream);
+                                   overflow_list, overflow_n, eig_fail, stream, ev_tri, ev_ql);
 }
 
 }  // namespace lg

@@ -36,6 +36,7 @@ constexpr int kChunkA = 128 * 16 * 2;       // 4096 B: M=128 x K=16 bf16
 constexpr int kChunkB = 80 * 16 * 2;        // 2560 B: N=80 x K=16 bf16
 constexpr int kStageBytes = 4 * (kChunkA + kChunkB);  // 26624 B
 constexpr int kN = 80;
+constexpr int kDS = kN + 1;  // row stride of the accumulator copy in shared memory (odd: no bank conflicts)
 constexpr int kTmemCols = 128;
 constexpr int kQueueCap = kStageEntries + kThreads;
 constexpr long long kSpinLimit = 1ll << 24;  // ~1 s of polling
@@ -372,20 +373,20 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev
     const int last = (stage - 1) & 1;
     if (!mbar_wait(&mbar[last], phase[last])) ok = false;
     fence_after();
-    float* D = reinterpret_cast<float*>(stage_base);  // 128 x 80, reuses the stages
+    float* D = reinterpret_cast<float*>(stage_base);  // 128 x kDS, reuses the stages
     for (int c0 = 0; c0 < kN; c0 += 16) {
       float v[16];
       tmem_ld16(tmem_d + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) D[(warp * 32 + lane) * kN + c0 + i] = v[i];
+      for (int i = 0; i < 16; ++i) D[(warp * 32 + lane) * kDS + c0 + i] = v[i];
     }
     __syncthreads();
     for (int idx = tid; idx < k * k; idx += kThreads) {
       const int i = idx % k, j = idx / k;
-      C[idx] = (double)D[i * kN + j] + (double)D[(64 + i) * kN + j] + (double)D[(64 + j) * kN + i];
+      C[idx] = (double)D[i * kDS + j] + (double)D[(64 + i) * kDS + j] + (double)D[(64 + j) * kDS + i];
     }
     for (int i = tid; i < k; i += kThreads)
-      t[i] = (double)D[i * kN + 64] + (double)D[i * kN + 65] + (double)D[(64 + i) * kN + 64];
+      t[i] = (double)D[i * kDS + 64] + (double)D[i * kDS + 65] + (double)D[(64 + i) * kDS + 64];
   }
   if (!ok && tid == 0) s_fail = 1;
   fence_before();
@@ -408,6 +409,244 @@ void launch_gram_tc(const Geometry& g, const HxDev& hx, const ListDev& l, const 
   if (rec) r = *rec;
   cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   gram_tc_kernel<<<b.nsolves, tc::kThreads, smem, stream>>>(g, hx, l, b, axb, C, t, err, r);
+}
+
+}  // namespace lg
+
+namespace lg {
+
+// Streaming variant for the analysis path: the solve's records (ln p-bucketed,
+// see records_kernel) are consumed in fixed stages of 64 consecutive records,
+// zero-weight ones included (they add zero rows), so no compaction is needed
+// and the loads can run ahead: the records of stage s+2 and the Y rows of
+// stage s+1 are in flight while stage s is scaled, split and issued.
+__global__ void __launch_bounds__(tc::kThreads) gram_tc_stream_kernel(Geometry g, HxDev hx,
+                                                                     ListDev l, SolveBatch b,
+                                                                     const double* axb,
+                                                                     double* Cout, double* tout,
+                                                                     int* err, RecDev rec) {
+  using namespace tc;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* stage_base = smem_raw;
+  __shared__ uint64_t mbar[2];
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int r_ent[3][kStageEntries];
+  __shared__ float r_s[3][kStageEntries];   // sqrt(weight)
+  __shared__ float r_d[3][kStageEntries];   // sqrt(weight) * innovation
+  __shared__ float s_al;
+  __shared__ int s_fail;
+
+  const int s = blockIdx.x;
+  const int k = g.ens;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int col = b.first_col + s / b.levels;
+  const int kk = s % b.levels + 1;
+  const int64_t base = l.off[col];
+  const bool vertical = g.vert_dist > 0.0;
+  if (tid == 0) {
+    s_fail = 0;
+    s_al = 0.0f;
+    if (vertical) {
+      const int glat = col % g.num_lat + 1, glon = col / g.num_lat + 1;
+      const size_t ci = (size_t)(glat - 1 + g.halo) +
+                        (size_t)(g.num_lat + 2 * g.halo) * (size_t)(glon - 1 + g.halo);
+      const double aps = axb[g.ps_row + (size_t)g.n * ci];
+      auto lev = [&](int k1) {
+        if (g.vcoord == LG_VCOORD_SIGMA) return g.ca[k1 - 1] * (aps - g.ptop) + g.ptop;
+        return g.ca[k1 - 1] * (g.p0 - g.ptop) + g.cb[k1 - 1] * (aps - g.ptop) + g.ptop;
+      };
+      s_al = (float)log(0.5 * (lev(kk) + lev(kk + 1)));
+    }
+  }
+  for (int i = tid; i < 2 * kStageBytes / 16; i += kThreads)
+    reinterpret_cast<uint4*>(stage_base)[i] = make_uint4(0, 0, 0, 0);
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_sh)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem_d = tmem_base_sh;
+  const float al = s_al;
+  const float inv_vd = vertical ? (float)(1.0 / g.vert_dist) : 0.0f;
+  // record window of this level
+  int w0 = 0, w1 = l.cnt[col];
+  if (vertical) {
+    const float span = 2.0f * (float)g.vert_dist;
+    int b_lo = (int)floorf((al - span - rec.lo) * rec.inv_dz) - 1;
+    int b_hi = (int)floorf((al + span - rec.lo) * rec.inv_dz) + 1;
+    b_lo = b_lo < 0 ? 0 : (b_lo > rec.nb - 1 ? rec.nb - 1 : b_lo);
+    b_hi = b_hi < 0 ? 0 : (b_hi > rec.nb - 1 ? rec.nb - 1 : b_hi);
+    const int* bo = rec.boff + (size_t)col * (rec.nb + 1);
+    w0 = bo[b_lo];
+    w1 = bo[b_hi + 1];
+  }
+  const int nrec = w1 - w0;
+  const int nst = (nrec + kStageEntries - 1) / kStageEntries;
+  const int m = tid & 63, g0 = tid >> 6;
+
+  // records of stage st into buffer st % 3 by warp wq (two records per lane)
+  auto load_records = [&](int st) {
+    const int buf = st % 3;
+    for (int e = lane; e < kStageEntries; e += 32) {
+      const int i = w0 + st * kStageEntries + e;
+      int ent = 0;
+      float sw = 0.0f, sd = 0.0f;
+      if (i < w1) {
+        ent = rec.ent[base + i];
+        float w = rec.w[base + i];
+        if (vertical) {
+          const float z = fabsf(al - rec.lnp[base + i]) * inv_vd;
+          w *= g.gc_filter_vertical ? schr2f(z) : (z > 2.0f ? 0.0f : 1.0f);
+        }
+        if (w > 0.0f) {
+          sw = sqrtf(w);
+          sd = (float)hx.dis[ent] * sw;
+        }
+      }
+      r_ent[buf][e] = ent;
+      r_s[buf][e] = sw;
+      r_d[buf][e] = sd;
+    }
+  };
+  // this thread's 32 raw Y values (member m) of stage st
+  auto load_y = [&](int st, float* v) {
+    const int buf = st % 3;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) {
+        const int e = (g0 + 2 * j) * 8 + jj;
+        v[j * 8 + jj] = (m < k && r_s[buf][e] > 0.0f)
+                            ? hx.yb32[(size_t)r_ent[buf][e] * k + m] : 0.0f;
+      }
+  };
+
+  float cur[32], nxt[32];
+  uint32_t phase[2] = {0u, 0u};
+  bool ok = true;
+  if (nst > 0) {
+    if (warp == 0) load_records(0);
+    if (warp == 1 && nst > 1) load_records(1);
+    __syncthreads();
+    load_y(0, cur);
+  }
+  for (int st = 0; st < nst; ++st) {
+    if (st + 1 < nst) load_y(st + 1, nxt);
+    if (st + 2 < nst && warp == (st & 3)) load_records(st + 2);
+    const int buf = st & 1;
+    if (st >= 2) {
+      if (!mbar_wait(&mbar[buf], phase[buf])) ok = false;
+      phase[buf] ^= 1u;
+    }
+    unsigned char* A = stage_base + buf * kStageBytes;
+    unsigned char* B = A + 4 * kChunkA;
+    const int rb = st % 3;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gi = g0 + 2 * j;
+      uint32_t hi[4], lo[4];
+#pragma unroll
+      for (int jj = 0; jj < 8; jj += 2) {
+        const float v0 = cur[j * 8 + jj] * r_s[rb][gi * 8 + jj];
+        const float v1 = cur[j * 8 + jj + 1] * r_s[rb][gi * 8 + jj + 1];
+        __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
+        const float2 hf = __bfloat1622float2(h2);
+        hi[jj / 2] = *reinterpret_cast<uint32_t*>(&h2);
+        lo[jj / 2] = pack_bf16(v0 - hf.x, v1 - hf.y);
+      }
+      const int chunk = gi >> 1, kc = gi & 1;
+      const int off_row = (m >> 3) * 256 + kc * 128 + (m & 7) * 16;
+      const int mlo = m + 64;
+      const int off_lo = (mlo >> 3) * 256 + kc * 128 + (mlo & 7) * 16;
+      *reinterpret_cast<uint4*>(A + chunk * kChunkA + off_row) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+      *reinterpret_cast<uint4*>(A + chunk * kChunkA + off_lo) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      *reinterpret_cast<uint4*>(B + chunk * kChunkB + off_row) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    }
+    if (tid < 8) {
+      const int gi = tid;
+      uint32_t hi[4], lo[4];
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        const float d0 = r_d[rb][gi * 8 + j], d1 = r_d[rb][gi * 8 + j + 1];
+        __nv_bfloat162 h2 = __floats2bfloat162_rn(d0, d1);
+        const float2 hf = __bfloat1622float2(h2);
+        hi[j / 2] = *reinterpret_cast<uint32_t*>(&h2);
+        lo[j / 2] = pack_bf16(d0 - hf.x, d1 - hf.y);
+      }
+      const int chunk = gi >> 1, kc = gi & 1;
+      const int r64 = 8 * 256 + kc * 128, r65 = 8 * 256 + kc * 128 + 16;
+      *reinterpret_cast<uint4*>(B + chunk * kChunkB + r64) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+      *reinterpret_cast<uint4*>(B + chunk * kChunkB + r65) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      fence_after();
+      const uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const uint64_t da = make_desc(a0 + c * kChunkA, 128, 256);
+        const uint64_t db = make_desc(b0 + c * kChunkB, 128, 256);
+        mma_bf16(tmem_d, da, db, (st > 0 || c > 0) ? 1u : 0u);
+      }
+      mma_commit(&mbar[buf]);
+    }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) cur[i] = nxt[i];
+  }
+
+  double* C = Cout + (size_t)s * k * k;
+  double* t = tout + (size_t)s * k;
+  if (nst == 0) {
+    for (int i = tid; i < k * k; i += kThreads) C[i] = 0.0;
+    for (int i = tid; i < k; i += kThreads) t[i] = 0.0;
+  } else {
+    const int last = (nst - 1) & 1;
+    if (!mbar_wait(&mbar[last], phase[last])) ok = false;
+    fence_after();
+    float* D = reinterpret_cast<float*>(stage_base);
+    for (int c0 = 0; c0 < kN; c0 += 16) {
+      float v[16];
+      tmem_ld16(tmem_d + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) D[(warp * 32 + lane) * kDS + c0 + i] = v[i];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < k * k; idx += kThreads) {
+      const int i = idx % k, j = idx / k;
+      C[idx] = (double)D[i * kDS + j] + (double)D[(64 + i) * kDS + j] + (double)D[(64 + j) * kDS + i];
+    }
+    for (int i = tid; i < k; i += kThreads)
+      t[i] = (double)D[i * kDS + 64] + (double)D[i * kDS + 65] + (double)D[(64 + i) * kDS + 64];
+  }
+  if (!ok && tid == 0) s_fail = 1;
+  fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d),
+                 "r"(kTmemCols));
+  if (s_fail && tid == 0) atomicExch(err, LG_ERR_TIMEOUT);
+  if (b.work && tid == 0) atomicAdd(b.work, (unsigned long long)nrec);
+}
+
+void launch_gram_tc_stream(const Geometry& g, const HxDev& hx, const ListDev& l,
+                           const SolveBatch& b, const double* axb, double* C, double* t, int* err,
+                           const RecDev& rec, cudaStream_t stream) {
+  if (b.nsolves == 0) return;
+  const size_t smem = 2 * tc::kStageBytes + 1024;
+  cudaFuncSetAttribute(gram_tc_stream_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  gram_tc_stream_kernel<<<b.nsolves, tc::kThreads, smem, stream>>>(g, hx, l, b, axb, C, t, err,
+                                                                   rec);
 }
 
 }  // namespace lg

@@ -145,6 +145,21 @@ bool gram_tc_supported(int ens);
 void launch_gram_tc(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
                     const double* axb, double* C, double* t, int* err, cudaStream_t stream,
                     const RecDev* rec = nullptr);
+// Records a timing event on st.  Inside a stream capture a plain cudaEventRecord
+// only orders the capture and is never recorded when the graph runs, so there
+// the event becomes an external event-record node of the graph; outside a
+// capture the external flag is not allowed and a plain record is made.
+inline cudaError_t record_event(cudaEvent_t e, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  const cudaError_t q = cudaStreamIsCapturing(st, &cs);
+  if (q != cudaSuccess) return q;
+  return cs == cudaStreamCaptureStatusActive
+             ? cudaEventRecordWithFlags(e, st, cudaEventRecordExternal)
+             : cudaEventRecord(e, st);
+}
+void launch_gram_tc_stream(const Geometry& g, const HxDev& hx, const ListDev& l,
+                           const SolveBatch& b, const double* axb, double* C, double* t, int* err,
+                           const RecDev& rec, cudaStream_t stream);
 void launch_records(int ncol, const ListDev& l, const HxDev& hx, float lo, float inv_dz, int nb,
                     int* boff, int* rec_ent, float* rec_lnp, float* rec_w, cudaStream_t stream);
 void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
@@ -156,7 +171,8 @@ void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const 
                  const double* xb, const double* axb, double* xa, double* axa, double* tri,
                  double* lam, void* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
                  int* overflow_list, int* overflow_n, int* eig_fail, bool fp32_vectors,
-                 cudaStream_t stream);
+                 cudaStream_t stream, cudaEvent_t ev_after_tri = nullptr,
+                 cudaEvent_t ev_after_ql = nullptr);
 void launch_split_mean(int ens, int64_t npts_rows, const double* xb_in, double* xb, double* axb,
                        int* err, cudaStream_t stream);
 void launch_post(int ens, int n, int num_lat, int num_lon, int halo, double gamma1, double gamma2,

@@ -72,6 +72,8 @@ class LgStats(C.Structure):
         ("ms_hx", C.c_double), ("ms_search", C.c_double), ("ms_solve", C.c_double),
         ("ms_total", C.c_double), ("ms_gram", C.c_double), ("ms_eig", C.c_double),
         ("n_launches", C.c_int64), ("n_gram_entries", C.c_int64),
+        ("ms_tridiag", C.c_double), ("ms_ql", C.c_double), ("ms_vec", C.c_double),
+        ("n_chunks", C.c_int64),
     ]
 
     def as_dict(self):

@@ -137,6 +137,10 @@ typedef struct lg_stats {
   double ms_eig;            /* sum of eigensolve+update launch durations */
   int64_t n_launches;       /* kernels this library launched in the last lg_run */
   int64_t n_gram_entries;   /* sum over solves of nonzero-weight entries (Gram work) */
+  double ms_tridiag;        /* eigensolve split: Householder reduction kernels */
+  double ms_ql;             /* implicit QL kernels */
+  double ms_vec;            /* vector transform + update kernels (incl. overflow fallback) */
+  int64_t n_chunks;         /* solve chunks (launches of each solve-phase kernel) */
 } lg_stats;
 
 typedef struct lg_ctx lg_ctx;

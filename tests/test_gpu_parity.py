@@ -156,3 +156,45 @@ def test_linear_and_cell_indexed_selection_agree(monkeypatch):
         ctx.letkf_final()
     (c0, e0, r0), (c1, e1, r1) = out
     assert np.array_equal(c0, c1) and np.array_equal(e0, e1) and np.array_equal(r0, r1)
+
+
+def test_repeated_runs_replay_the_captured_graph():
+    """The first lg_run captures the analysis into a CUDA graph and later runs
+    replay it; a second background through the same context must still match
+    the oracle, and an eager run (LETKF_GB300_NO_GRAPH) must agree bit for bit."""
+    import os
+    import letkf_gb300 as lg
+    import synth
+    from oracle import oracle as orc
+
+    cfg = lg.preset("tiny3d")
+    w = synth.make_workload(cfg)
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    o = orc.Oracle(cfg, w.obs)
+    results = []
+    for scale in (1.0, 1.3):
+        xb = np.ascontiguousarray(w.xb * scale)
+        xa = np.zeros_like(xb)
+        axa = np.zeros_like(w.axb)
+        ctx.letkf_run(0, xb, w.axb, xa, axa)
+        o.hx(xb, w.axb)
+        xa_o = np.zeros_like(xb)
+        axa_o = np.zeros_like(w.axb)
+        o.analysis(xb, w.axb, xa_o, axa_o)
+        w2 = synth.Workload(cfg, xb, w.axb, w.truth, w.obs)
+        assert _rel_err(cfg, w2, (xa, axa), (xa_o, axa_o)) < RTOL_ANALYSIS
+        results.append((xa.copy(), axa.copy()))
+    ctx.letkf_final()
+    os.environ["LETKF_GB300_NO_GRAPH"] = "1"
+    try:
+        ctx = lg.Letkf(cfg)
+        ctx.set_obs(w.obs)
+        xb = np.ascontiguousarray(w.xb * 1.3)
+        xa = np.zeros_like(xb)
+        axa = np.zeros_like(w.axb)
+        ctx.letkf_run(0, xb, w.axb, xa, axa)
+        assert np.array_equal(xa, results[1][0]) and np.array_equal(axa, results[1][1])
+        ctx.letkf_final()
+    finally:
+        del os.environ["LETKF_GB300_NO_GRAPH"]

@@ -52,6 +52,10 @@ def parse():
                     help="target CPU time of the bounded oracle sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--tune", default="",
+                    help="launch settings before timing, e.g. chunk_mb=2048,solve_streams=2")
+    ap.add_argument("--autotune", action="store_true",
+                    help="run lg_autotune on the workload (untimed) before the warm-up")
     return ap.parse_args()
 
 
@@ -238,6 +242,11 @@ def main():
     xa = torch.zeros_like(xb)
     axa = torch.zeros_like(axb)
     stream = torch.cuda.current_stream(dev)
+    if args.tune:
+        ctx.set_tuning(**{kv.split("=")[0]: int(kv.split("=")[1]) for kv in args.tune.split(",")})
+    if args.autotune:
+        ctx.autotune(xb, axb, xa, axa, stream.cuda_stream)
+    tuning = ctx.tuning()
 
     def step():
         ctx.letkf_run_device(0, xb, axb, xa, axa, stream.cuda_stream)
@@ -319,7 +328,8 @@ def main():
                    "columns": ncol, "solves_per_step": st["n_solves"],
                    "local_entries_per_step": st["nobsl_total"],
                    "l2": "inputs (background 3.4 GB) larger than L2; no flush",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "tuning": {kk: v for kk, v in tuning.items() if kk != "ms"}},
         "clocks": clocks,
         "gpu_launches": acc["n_launches"],
         "phases_ms": {n: round(v["ms_per_step"], 3) for n, v in kernels.items()},

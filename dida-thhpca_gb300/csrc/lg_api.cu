@@ -18,6 +18,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <initializer_list>
+
 #include <algorithm>
 #include <vector>
 
@@ -58,21 +60,30 @@ struct lg_ctx {
   size_t scan_tmp_bytes = 0;
   int64_t list_total = 0;
   // solve workspace
-  double *d_C = nullptr, *d_t = nullptr;
-  size_t solve_cap = 0;
-  // lane-parallel eigensolver scratch (tridiagonal form, eigenvalues, rotation log)
-  double *d_tri = nullptr, *d_lam = nullptr;
-  double2* d_rot_cs = nullptr;
-  unsigned char* d_rot_i = nullptr;
-  int *d_rot_n = nullptr, *d_ovf_list = nullptr;
+  // per solve stream: Gram matrices and projected innovations of a chunk, and
+  // the lane-parallel eigensolver's scratch (tridiagonal form, eigenvalues,
+  // rotation log, overflow list and count)
+  struct SolveLane {
+    double *C = nullptr, *t = nullptr, *tri = nullptr, *lam = nullptr;
+    double2* rot_cs = nullptr;
+    unsigned char* rot_i = nullptr;
+    int *rot_n = nullptr, *ovf_list = nullptr, *ovf_n = nullptr;
+    size_t cap = 0;        // solves
+    size_t rot_n_cap = 0;  // rotation-log entries per solve it was sized for
+  };
+  SolveLane lane[2];
   int rot_cap = 0;
+  cudaStream_t side_stream = nullptr;  // second solve stream (tune.solve_streams = 2)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // ln p bucketed records for the mixed-precision Gram
-  int* d_rec_ent = nullptr;
-  float *d_rec_lnp = nullptr, *d_rec_w = nullptr;
+  float4* d_rec = nullptr;
   int* d_boff = nullptr;
   size_t rec_cap = 0;
-  float lnp_lo = 0.0f, lnp_inv_dz = 1.0f;
-  static constexpr int kLnpBuckets = 128;
+  float lnp_lo = 0.0f;
+  double lnp_span = 1.0;
+  int boff_nb = 0;  // bucket count d_boff was sized for
+  // launch shapes and bucket boundaries (lg_set_tuning / lg_autotune)
+  lg_tuning tune{1024, LG_GRAM_AUTO, 128, 1, 4, 2, 0.0};
   // status words: [0] err, [1] eig_fail
   int* d_status = nullptr;
   unsigned long long* d_band = nullptr;
@@ -328,7 +339,15 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   lg_ctx* c = new lg_ctx();
   c->cfg = g;
   cudaGetDevice(&c->dev);
-  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  if (c->side_stream) cudaStreamDestroy(c->side_stream);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side_stream) cudaStreamDestroy(c->side_stream);
     delete c;
     return LG_ERR_CUDA;
   }
@@ -581,7 +600,7 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
     if (!(hi >= lo)) lo = hi = 0.0;
     const double span = std::max(hi - lo, 1e-3) * (1.0 + 1e-6);
     c->lnp_lo = (float)(lo - 1e-6 * span);
-    c->lnp_inv_dz = (float)(lg_ctx::kLnpBuckets / span);
+    c->lnp_span = span;
   }
   c->types = tt;
   c->geo.n_types = T;
@@ -671,6 +690,8 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
 
 namespace {
 
+enum class GramKind { kColumn, kStream, kQueue };
+
 // Timing events of an analysis go through lg::record_event (lg_internal.h), which
 // keeps them valid inside a CUDA-graph capture.
 cudaError_t record_event(cudaEvent_t e, cudaStream_t st) { return lg::record_event(e, st); }
@@ -729,47 +750,51 @@ int prepare_capacity(lg_ctx* c) {
   }
   c->list_total = total;
   const bool mixed_tc = g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k);
-  if (mixed_tc && (c->rec_cap < c->list_cap || !c->d_boff)) {
-    dfree(c->d_rec_ent); dfree(c->d_rec_lnp); dfree(c->d_rec_w); dfree(c->d_boff);
+  if (mixed_tc && (c->rec_cap < c->list_cap || !c->d_boff || c->boff_nb != c->tune.lnp_buckets)) {
+    dfree(c->d_rec); dfree(c->d_boff);
     int r = LG_OK;
-    r |= dalloc(&c->d_rec_ent, c->list_cap);
-    r |= dalloc(&c->d_rec_lnp, c->list_cap);
-    r |= dalloc(&c->d_rec_w, c->list_cap);
-    r |= dalloc(&c->d_boff, (size_t)ncol * (lg_ctx::kLnpBuckets + 1));
-    if (r != LG_OK) { c->rec_cap = 0; return LG_ERR_NOMEM; }
+    r |= dalloc(&c->d_rec, c->list_cap);
+    r |= dalloc(&c->d_boff, (size_t)ncol * (c->tune.lnp_buckets + 1));
+    if (r != LG_OK) { c->rec_cap = 0; c->boff_nb = 0; return LG_ERR_NOMEM; }
     c->rec_cap = c->list_cap;
+    c->boff_nb = c->tune.lnp_buckets;
   }
-  // solve chunks bounded by the Gram workspace (1 GiB; LETKF_GB300_CHUNK_MB overrides
-  // it, e.g. to keep a profiler capture's device footprint small)
+  // solve chunks bounded by the Gram workspace (tune.chunk_mb; LETKF_GB300_CHUNK_MB
+  // overrides it, e.g. to keep a profiler capture's device footprint small)
   const int levels = g.vert_dist > 0.0 ? g.nz : 1;
   const size_t per_col = (size_t)levels * k * k * sizeof(double);
-  size_t budget = (size_t)1 << 30;
+  size_t budget = (size_t)c->tune.chunk_mb << 20;
   if (const char* env = getenv("LETKF_GB300_CHUNK_MB")) budget = (size_t)std::max(1, atoi(env)) << 20;
   c->chunk = (int)std::min<size_t>((size_t)ncol, std::max<size_t>(1, budget / per_col));
   c->use_eig2 = lg::eig2_supported(geo);
-  if ((size_t)c->chunk * levels > c->solve_cap) {
-    dfree(c->d_C); dfree(c->d_t); dfree(c->d_tri); dfree(c->d_lam); dfree(c->d_rot_cs);
-    dfree(c->d_rot_i); dfree(c->d_rot_n); dfree(c->d_ovf_list);
-    const size_t cap = (size_t)c->chunk * levels;
-    c->rot_cap = 3 * k * k;
-    // test hook: a small log forces the overflow fallback path
-    if (const char* env = getenv("LETKF_GB300_ROT_CAP")) c->rot_cap = std::max(1, atoi(env));
+  c->rot_cap = 3 * k * k;
+  // test hook: a small log forces the overflow fallback path
+  if (const char* env = getenv("LETKF_GB300_ROT_CAP")) c->rot_cap = std::max(1, atoi(env));
+  const int nl = c->tune.solve_streams;
+  for (int li = 0; li < 2; ++li) {
+    lg_ctx::SolveLane& L = c->lane[li];
+    const size_t cap = li < nl ? (size_t)c->chunk * levels : 0;
+    if (L.cap >= cap && (cap > 0 || L.cap == 0) && L.rot_n_cap == (size_t)c->rot_cap) continue;
+    dfree(L.C); dfree(L.t); dfree(L.tri); dfree(L.lam); dfree(L.rot_cs); dfree(L.rot_i);
+    dfree(L.rot_n); dfree(L.ovf_list); dfree(L.ovf_n);
+    L.cap = 0;
+    L.rot_n_cap = 0;
+    if (cap == 0) continue;
     int r = LG_OK;
-    r |= dalloc(&c->d_C, cap * k * k);
-    r |= dalloc(&c->d_t, cap * k);
+    r |= dalloc(&L.C, cap * k * k);
+    r |= dalloc(&L.t, cap * k);
+    r |= dalloc(&L.ovf_n, 1);
     if (c->use_eig2) {
-      r |= dalloc(&c->d_tri, cap * lg::eig2_tri_doubles(k));
-      r |= dalloc(&c->d_lam, cap * k);
-      r |= dalloc(&c->d_rot_cs, cap * (size_t)c->rot_cap);
-      r |= dalloc(&c->d_rot_i, cap * (size_t)c->rot_cap);
-      r |= dalloc(&c->d_rot_n, cap);
-      r |= dalloc(&c->d_ovf_list, cap);
+      r |= dalloc(&L.tri, cap * lg::eig2_tri_doubles(k));
+      r |= dalloc(&L.lam, cap * k);
+      r |= dalloc(&L.rot_cs, cap * (size_t)c->rot_cap);
+      r |= dalloc(&L.rot_i, cap * (size_t)c->rot_cap);
+      r |= dalloc(&L.rot_n, cap);
+      r |= dalloc(&L.ovf_list, cap);
     }
-    if (r != LG_OK) {
-      c->solve_cap = 0;
-      return LG_ERR_NOMEM;
-    }
-    c->solve_cap = cap;
+    if (r != LG_OK) return LG_ERR_NOMEM;
+    L.cap = cap;
+    L.rot_n_cap = (size_t)c->rot_cap;
   }
   const int nchunks = (ncol + c->chunk - 1) / c->chunk;
   while ((int)c->kev.size() < 5 * nchunks) {
@@ -814,22 +839,41 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   const bool mixed_tc = g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k);
   lg::RecDev rec{};
   if (mixed_tc) {
-    lg::launch_records(ncol, c->lists, c->hx, c->lnp_lo, c->lnp_inv_dz, lg_ctx::kLnpBuckets,
-                       c->d_boff, c->d_rec_ent, c->d_rec_lnp, c->d_rec_w, st);
+    const int nb = c->tune.lnp_buckets;
+    const float inv_dz = (float)(nb / c->lnp_span);
+    lg::launch_records(ncol, c->lists, c->hx, c->lnp_lo, inv_dz, nb,
+                       c->d_boff, c->d_rec, st);
     launches += 1;
-    rec.ent = c->d_rec_ent;
-    rec.lnp = c->d_rec_lnp;
-    rec.w = c->d_rec_w;
+    rec.r = c->d_rec;
     rec.boff = c->d_boff;
-    rec.nb = lg_ctx::kLnpBuckets;
+    rec.nb = nb;
     rec.lo = c->lnp_lo;
-    rec.inv_dz = c->lnp_inv_dz;
+    rec.inv_dz = inv_dz;
   }
   CK(record_event(c->ev[2], st));
   const int levels = g.vert_dist > 0.0 ? g.nz : 1;
   const int chunk = c->chunk;
   const int nchunks = (ncol + chunk - 1) / chunk;
+  // tensor-core Gram variant: column groups (default), one CTA per solve
+  // streaming its records, or one CTA per solve with a compaction queue
+  GramKind gram_kind = lg::gram_col_supported(k) ? GramKind::kColumn : GramKind::kStream;
+  if (c->tune.gram_kernel == LG_GRAM_STREAM) gram_kind = GramKind::kStream;
+  if (c->tune.gram_kernel == LG_GRAM_QUEUE) gram_kind = GramKind::kQueue;
+  if (const char* e = getenv("LETKF_GB300_GRAM")) {
+    if (!strcmp(e, "stream")) gram_kind = GramKind::kStream;
+    if (!strcmp(e, "queue")) gram_kind = GramKind::kQueue;
+  }
+  // chunks alternate between the solve streams; each stream reuses its own
+  // scratch, so the Gram of one chunk can run beside the eigensolve of another
+  const int nl = c->tune.solve_streams;
+  cudaStream_t ss[2] = {st, c->side_stream};
+  if (nl == 2) {
+    CK(cudaEventRecord(c->ev_fork, st));
+    CK(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
+  }
   for (int q = 0; q < nchunks; ++q) {
+    lg_ctx::SolveLane& L = c->lane[q % nl];
+    cudaStream_t s = ss[q % nl];
     lg::SolveBatch b{};
     b.mode = 0;
     b.first_col = q * chunk;
@@ -837,36 +881,42 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     b.levels = levels;
     b.nsolves = b.ncols * levels;
     b.work = c->d_work;
-    CK(record_event(c->kev[5 * q], st));
-    if (mixed_tc && !getenv("LETKF_GB300_GRAM_QUEUE"))
-      lg::launch_gram_tc_stream(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, c->d_status, rec, st);
+    CK(record_event(c->kev[5 * q], s));
+    if (mixed_tc && gram_kind == GramKind::kColumn)
+      lg::launch_gram_col(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec, s);
+    else if (mixed_tc && gram_kind == GramKind::kStream)
+      lg::launch_gram_tc_stream(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec, s);
     else if (mixed_tc)
-      lg::launch_gram_tc(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, c->d_status, st, &rec);
+      lg::launch_gram_tc(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, s, &rec);
     else
-      lg::launch_gram64(geo, c->hx, c->lists, b, axb, c->d_C, c->d_t, st);
-    CK(cudaMemsetAsync(c->d_status + 2, 0, sizeof(int), st));
-    CK(record_event(c->kev[5 * q + 1], st));
+      lg::launch_gram64(geo, c->hx, c->lists, b, axb, L.C, L.t, s);
+    CK(cudaMemsetAsync(L.ovf_n, 0, sizeof(int), s));
+    CK(record_event(c->kev[5 * q + 1], s));
     if (c->use_eig2) {
-      lg::launch_eig2(geo, b, c->d_C, c->d_t, xb, axb, xa, axa, c->d_tri, c->d_lam, c->d_rot_cs,
-                      c->d_rot_i, c->d_rot_n, c->rot_cap, c->d_ovf_list, c->d_status + 2,
-                      c->d_status + 1, g.precision == LG_PREC_MIXED, st, c->kev[5 * q + 2],
-                      c->kev[5 * q + 3]);
+      lg::launch_eig2(geo, b, L.C, L.t, xb, axb, xa, axa, L.tri, L.lam, L.rot_cs, L.rot_i,
+                      L.rot_n, c->rot_cap, L.ovf_list, L.ovf_n, c->d_status + 1,
+                      g.precision == LG_PREC_MIXED, c->tune.ql_warps, c->tune.vec_warps, s,
+                      c->kev[5 * q + 2], c->kev[5 * q + 3]);
       // matrices whose rotation log overflowed: accumulate-eigenvector solver
       lg::SolveBatch fb = b;
-      fb.solve_list = c->d_ovf_list;
-      fb.solve_count = c->d_status + 2;
-      lg::launch_eig_apply(geo, fb, c->d_C, c->d_t, xb, axb, xa, axa, nullptr, nullptr,
-                           c->d_status + 1, st);
+      fb.solve_list = L.ovf_list;
+      fb.solve_count = L.ovf_n;
+      lg::launch_eig_apply(geo, fb, L.C, L.t, xb, axb, xa, axa, nullptr, nullptr,
+                           c->d_status + 1, s);
       launches += 4;
     } else {
-      lg::launch_eig_apply(geo, b, c->d_C, c->d_t, xb, axb, xa, axa, nullptr, nullptr,
-                           c->d_status + 1, st);
-      CK(record_event(c->kev[5 * q + 2], st));
-      CK(record_event(c->kev[5 * q + 3], st));
+      lg::launch_eig_apply(geo, b, L.C, L.t, xb, axb, xa, axa, nullptr, nullptr,
+                           c->d_status + 1, s);
+      CK(record_event(c->kev[5 * q + 2], s));
+      CK(record_event(c->kev[5 * q + 3], s));
       launches += 1;
     }
-    CK(record_event(c->kev[5 * q + 4], st));
+    CK(record_event(c->kev[5 * q + 4], s));
     launches += 1;
+  }
+  if (nl == 2) {
+    CK(cudaEventRecord(c->ev_join, c->side_stream));
+    CK(cudaStreamWaitEvent(st, c->ev_join, 0));
   }
   CK(record_event(c->ev[3], st));
   CK(cudaGetLastError());
@@ -1069,6 +1119,92 @@ int lg_run_da_parallel(lg_ctx* c, int ntimes, double gamma1, double gamma2, doub
   return LG_OK;
 }
 
+int lg_get_tuning(const lg_ctx* c, lg_tuning* out) {
+  if (!c || !out) return LG_ERR_ARG;
+  *out = c->tune;
+  return LG_OK;
+}
+
+int lg_set_tuning(lg_ctx* c, const lg_tuning* t) {
+  if (!c || !t) return LG_ERR_ARG;
+  if (t->chunk_mb < 16 || t->chunk_mb > 65536 || t->gram_kernel < LG_GRAM_AUTO ||
+      t->gram_kernel > LG_GRAM_QUEUE || t->lnp_buckets < 8 || t->lnp_buckets > 1024 ||
+      t->ql_warps < 1 || t->ql_warps > 6 || t->vec_warps < 1 || t->vec_warps > 8 ||
+      t->solve_streams < 1 || t->solve_streams > 2)
+    return LG_ERR_ARG;
+  c->tune = *t;
+  c->capacity_ready = false;  // chunk size and bucket count size buffers
+  drop_graph(c);
+  return LG_OK;
+}
+
+int lg_autotune(lg_ctx* c, const double* xb, const double* axb, double* xa, double* axa,
+                void* stream, lg_tuning* best) {
+  if (!c || !xb || !axb || !xa || !axa || !best) return LG_ERR_ARG;
+  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
+  const lg_config& g = c->cfg;
+  const bool mixed = g.precision == LG_PREC_MIXED;
+  const bool vertical = g.vert_dist > 0.0;
+  lg_tuning cur = c->tune;
+  if (cur.gram_kernel == LG_GRAM_AUTO)
+    cur.gram_kernel = lg::gram_col_supported(g.ens) ? LG_GRAM_COLUMN : LG_GRAM_STREAM;
+  // one untimed analysis (buffer sizing, graph capture), then the faster of two
+  auto measure = [&](const lg_tuning& t, double* ms) -> int {
+    int r = lg_set_tuning(c, &t);
+    if (r != LG_OK) return r;
+    if ((r = lg_run_device(c, 0, xb, axb, xa, axa, stream)) != LG_OK) return r;
+    double m = 1e300;
+    for (int rep = 0; rep < 2; ++rep) {
+      if ((r = lg_run_device(c, 0, xb, axb, xa, axa, stream)) != LG_OK) return r;
+      m = std::min(m, c->stats.ms_total);
+    }
+    *ms = m;
+    return LG_OK;
+  };
+  double best_ms = 0.0;
+  int r = measure(cur, &best_ms);
+  if (r != LG_OK) return r;
+  auto try_param = [&](int lg_tuning::*field, std::initializer_list<int> cands) -> int {
+    for (int v : cands) {
+      if (cur.*field == v) continue;
+      lg_tuning t = cur;
+      t.*field = v;
+      double ms = 0.0;
+      const int rr = measure(t, &ms);
+      if (rr == LG_ERR_NOMEM) {  // the candidate does not fit next to the resident data
+        cudaGetLastError();
+        continue;
+      }
+      if (rr != LG_OK) return rr;
+      if (ms < best_ms) {
+        best_ms = ms;
+        cur = t;
+      }
+    }
+    return LG_OK;
+  };
+  if ((r = try_param(&lg_tuning::chunk_mb, {256, 512, 1024, 2048, 4096})) != LG_OK) return r;
+  if (mixed) {
+    if (lg::gram_col_supported(g.ens)) {
+      if ((r = try_param(&lg_tuning::gram_kernel, {LG_GRAM_COLUMN, LG_GRAM_STREAM, LG_GRAM_QUEUE})) != LG_OK)
+        return r;
+    } else if ((r = try_param(&lg_tuning::gram_kernel, {LG_GRAM_STREAM, LG_GRAM_QUEUE})) != LG_OK) {
+      return r;
+    }
+    if (vertical && (r = try_param(&lg_tuning::lnp_buckets, {32, 64, 128, 256, 512})) != LG_OK)
+      return r;
+  }
+  if ((r = try_param(&lg_tuning::ql_warps, {1, 2, 4})) != LG_OK) return r;
+  if ((r = try_param(&lg_tuning::vec_warps, {2, 4, 8})) != LG_OK) return r;
+  if ((r = try_param(&lg_tuning::solve_streams, {1, 2})) != LG_OK) return r;
+  cur.ms = best_ms;
+  if ((r = lg_set_tuning(c, &cur)) != LG_OK) return r;
+  // leave the context sized and captured for the chosen settings
+  if ((r = lg_run_device(c, 0, xb, axb, xa, axa, stream)) != LG_OK) return r;
+  *best = cur;
+  return LG_OK;
+}
+
 int lg_get_stats(const lg_ctx* c, lg_stats* st) {
   if (!c || !st) return LG_ERR_ARG;
   *st = c->stats;
@@ -1120,10 +1256,12 @@ void lg_destroy(lg_ctx* c) {
   dfree(c->lists.cnt); dfree(c->lists.off); dfree(c->lists.ent); dfree(c->lists.rloc);
   dfree(c->lists.capped);
   if (c->d_scan_tmp) cudaFree(c->d_scan_tmp);
-  dfree(c->d_C); dfree(c->d_t); dfree(c->d_status); dfree(c->d_band);
-  dfree(c->d_tri); dfree(c->d_lam); dfree(c->d_rot_cs); dfree(c->d_rot_i); dfree(c->d_rot_n);
-  dfree(c->d_ovf_list);
-  dfree(c->d_rec_ent); dfree(c->d_rec_lnp); dfree(c->d_rec_w); dfree(c->d_boff);
+  for (auto& L : c->lane) {
+    dfree(L.C); dfree(L.t); dfree(L.tri); dfree(L.lam); dfree(L.rot_cs); dfree(L.rot_i);
+    dfree(L.rot_n); dfree(L.ovf_list); dfree(L.ovf_n);
+  }
+  dfree(c->d_status); dfree(c->d_band);
+  dfree(c->d_rec); dfree(c->d_boff);
   dfree(c->d_xb); dfree(c->d_axb); dfree(c->d_xa); dfree(c->d_axa);
   dfree(c->d_xin); dfree(c->d_spb); dfree(c->d_spa);
   for (auto& e : c->ev)

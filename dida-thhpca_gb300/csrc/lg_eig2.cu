@@ -28,6 +28,8 @@
 // holds is flagged and redone by eig_apply_kernel (lg_eig.cu).
 #include <float.h>
 
+#include <algorithm>
+
 #include "lg_device.cuh"
 #include "lg_internal.h"
 
@@ -194,7 +196,7 @@ __device__ inline float2 make_rot<float2>(double c, double s) { return make_floa
 // LT: element type of the rotation log (double2 for the FP64 path, float2 when the
 // rotations are only replayed in FP32 by the mixed-precision vector kernel)
 template <typename LT>
-__global__ void __launch_bounds__(128) ql_kernel(int n, int nsolves, double shift,
+__global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shift,
                                                  const double* tri, double* lam, LT* rot_cs,
                                                  unsigned char* rot_i, int* rot_n, int rot_cap,
                                                  int* overflow_list, int* overflow_n,
@@ -307,7 +309,7 @@ __global__ void __launch_bounds__(128) ql_kernel(int n, int nsolves, double shif
 // VT: arithmetic of the vector transforms (double: FP64 path; float: the mixed
 // path's Xb.W contraction, with eigenvalues, rotations and reflectors from FP64)
 template <typename VT, typename LT>
-__global__ void __launch_bounds__(128) vec_kernel(Geometry g, SolveBatch b, const double* tin,
+__global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, const double* tin,
                                                   const double* tri, const double* lam,
                                                   const LT* rot_cs,
                                                   const unsigned char* rot_i, const int* rot_n,
@@ -454,9 +456,10 @@ template <typename VT, typename LT>
 void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
                    const double* xb, const double* axb, double* xa, double* axa, double* tri,
                    double* lam, LT* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
-                   int* overflow_list, int* overflow_n, int* eig_fail, cudaStream_t stream,
-                   cudaEvent_t ev_tri, cudaEvent_t ev_ql) {
+                   int* overflow_list, int* overflow_n, int* eig_fail, int ql_warps,
+                   int vec_warps, cudaStream_t stream, cudaEvent_t ev_tri, cudaEvent_t ev_ql) {
   const int n = g.ens;
+  constexpr size_t kSmemMax = 227 * 1024;
   const int ns = b.nsolves;
   if (ns == 0) return;
   // 1. tridiagonalisation
@@ -465,7 +468,7 @@ void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, cons
   tridiag_kernel<<<ns, 32, smem_t, stream>>>(n, ns, C, tri);
   if (ev_tri) record_event(ev_tri, stream);
   // 2. QL, one solve per lane
-  const int ql_warps = 1;
+  ql_warps = std::max(1, std::min(ql_warps, (int)(kSmemMax / (sizeof(double) * 64 * n))));
   const size_t smem_q = sizeof(double) * (size_t)ql_warps * 64 * n;
   cudaFuncSetAttribute(ql_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_q);
   const int ql_blocks = (ns + 32 * ql_warps - 1) / (32 * ql_warps);
@@ -477,7 +480,8 @@ void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, cons
   const bool vertical = g.vert_dist > 0.0;
   const int per = 1 + (vertical ? g.n_var : g.n);
   const int slots = 32 / per;
-  const int vwarps = 4;
+  const size_t vper = sizeof(VT) * ((size_t)32 * n + (size_t)slots * n);
+  const int vwarps = std::max(1, std::min(vec_warps, (int)(kSmemMax / vper)));
   const size_t smem_v = sizeof(VT) * ((size_t)vwarps * 32 * n + (size_t)vwarps * slots * n);
   cudaFuncSetAttribute(vec_kernel<VT, LT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_v);
@@ -490,15 +494,18 @@ void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const 
                  const double* xb, const double* axb, double* xa, double* axa, double* tri,
                  double* lam, void* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
                  int* overflow_list, int* overflow_n, int* eig_fail, bool fp32_vectors,
-                 cudaStream_t stream, cudaEvent_t ev_tri, cudaEvent_t ev_ql) {
+                 int ql_warps, int vec_warps, cudaStream_t stream, cudaEvent_t ev_tri,
+                 cudaEvent_t ev_ql) {
   if (fp32_vectors)
     launch_eig2_t<float, float2>(g, b, C, t, xb, axb, xa, axa, tri, lam,
                                  static_cast<float2*>(rot_cs), rot_i, rot_n, rot_cap,
-                                 overflow_list, overflow_n, eig_fail, stream, ev_tri, ev_ql);
+                                 overflow_list, overflow_n, eig_fail, ql_warps, vec_warps, stream,
+                                 ev_tri, ev_ql);
   else
     launch_eig2_t<double, double2>(g, b, C, t, xb, axb, xa, axa, tri, lam,
                                    static_cast<double2*>(rot_cs), rot_i, rot_n, rot_cap,
-                                   overflow_list, overflow_n, eig_fail, stream, ev_tri, ev_ql);
+                                   overflow_list, overflow_n, eig_fail, ql_warps, vec_warps,
+                                   stream, ev_tri, ev_ql);
 }
 
 }  // namespace lg

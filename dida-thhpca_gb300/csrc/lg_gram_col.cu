@@ -1,0 +1,501 @@
+// lg_gram_col.cu -- mixed-precision Gram matrices of a group of levels of one
+// grid column, with every observation's ensemble row read once for the group.
+//
+// The solves of one column at different levels share the column's neighbour
+// list; the vertical localisation only changes the weights (and which ln p
+// window of the bucketed records contributes).  Reading each record's ensemble
+// row once per level, as one CTA per solve does, re-reads the same rows about
+// as often as a record lies in the windows of neighbouring levels (~8 times at
+// 0.2 ln p and 32 levels).  Here one persistent CTA per SM takes work items
+// (column, group of up to kG = 8 consecutive levels):
+//
+//   producer warp   streams the union of the group's record windows in stages
+//                   of 64 records: the records (entry, ln p, rdiaginv*rloc, d)
+//                   to a shared ring, and the 64-member FP32 ensemble rows of
+//                   the entries with cp.async (16-byte chunks) into a Y ring of
+//                   kRing stages; completion is tracked per stage by an
+//                   mbarrier (cp.async.mbarrier.arrive.noinc).  The records of
+//                   the next stage are loaded while this stage's rows are issued.
+//   8 converter warps  each owns 16 records of a stage (two 8-record groups)
+//                   for all 64 members: per level whose window meets the stage
+//                   it computes its records' weights w = rdiaginv*rloc*GC_vertical,
+//                   splits y~ = sqrt(w) y into BF16 hi + lo and writes its part of
+//                   A = [hi; lo] (M = 128, K = 64, K-major no-swizzle) into one of
+//                   kOps operand buffers, then signals the buffer's mbarrier.
+//                   t = Y~^T d~ is accumulated in FP32 registers.
+//   MMA warp        waits for all eight parts of a buffer and issues four
+//                   tcgen05.mma (N = 64, B = the hi rows of A) into the level's
+//                   own 64 TMEM columns, committing to the buffer's mbarrier.
+// The converter warps never wait on each other inside an item; they meet on a
+// named barrier only for the epilogue, which copies the accumulators out.
+//
+//   C = D[0:64,:] + D[64:128,:] + D[64:128,:]^T   (hi hi + lo hi + hi lo), in FP32,
+//   then converted to FP64 -- the same quantities as lg_gram_tc.cu
+//   (letkf_core.F90:58-75,146-195).
+//
+// Every mbarrier wait is bounded; on expiry the CTA records LG_ERR_TIMEOUT,
+// raises a shared abort flag that ends every other wait at once, waits (bounded)
+// for its own MMAs and copies, frees its tensor memory and returns.
+#include <climits>
+
+#include "lg_device.cuh"
+#include "lg_internal.h"
+#include "lg_tc.cuh"
+
+namespace lg {
+namespace colk {
+
+constexpr int kConv = 256;                      // converter threads (warps 0-7)
+constexpr int kProducer = kConv / 32;           // warp 8
+constexpr int kMmaWarp = kProducer + 1;         // warp 9
+constexpr int kThreads = kConv + 64;
+constexpr int kG = 8;                           // levels per work item
+constexpr int kN = 64;                          // accumulator columns per level
+constexpr int kRing = 6;                        // Y / record stages in flight
+constexpr int kOps = 4;                         // operand (A) buffers
+constexpr int kRows = 64;                       // records per stage (4 MMAs of K = 16)
+constexpr int kChunkA = 128 * 16 * 2;           // 4096 B: M = 128 x K = 16 BF16
+constexpr int kOpBytes = 4 * kChunkA;           // 16 KB
+constexpr int kYBytes = kRows * 64 * 4;         // 16 KB: 64 rows of 64 FP32
+constexpr int kDS = kN + 1;                     // accumulator copy row stride (odd)
+constexpr int kOffY = 0;
+constexpr int kOffOps = kOffY + kRing * kYBytes;
+constexpr int kOffRec = kOffOps + kOps * kOpBytes;
+constexpr int kOffW = kOffRec + kRing * kRows * 16;
+constexpr int kOffEnd = kOffW + 8 * 2 * kG * 16 * 4;  // per-warp sqrt(w), sqrt(w) d
+constexpr int kSmemBytes = kOffEnd;
+static_assert(128 * kDS * 4 <= kOps * kOpBytes, "accumulator copy must fit the operand buffers");
+
+// instruction descriptor: kind::f16, BF16 A/B, FP32 D, K-major A and B, M = 128, N = 64
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
+                            ((uint32_t)(128 >> 4) << 24);
+
+__device__ inline void mma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ inline void arrive(uint64_t* bar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(
+                   tc::smem_u32(bar))
+               : "memory");
+}
+
+__device__ inline void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(dst)), "l"(src)
+               : "memory");
+}
+
+__device__ inline void cp_async_arrive(uint64_t* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(tc::smem_u32(bar))
+               : "memory");
+}
+
+__device__ inline void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+__device__ inline void conv_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kConv) : "memory"); }
+
+// Wait for a phase, suspending between polls; gives up after 2 s of wall time
+// (raising the CTA's abort flag) or as soon as another thread has given up.
+__device__ inline bool wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  if (tc::mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = tc::global_ns();
+  while (true) {
+    if (tc::mbar_try_wait_hint(bar, parity, 1000u)) return true;
+    if (*abort) return false;
+    if (tc::global_ns() - t0 > 2000000000ull) {
+      *abort = 1;
+      return false;
+    }
+  }
+}
+
+// ln p of level kk (1-based) at column col and its window [w0, w1) of records
+__device__ inline void level_window(const Geometry& g, const ListDev& l, const RecDev& rec,
+                                    const double* axb, int col, int kk, float& al, int& w0,
+                                    int& w1) {
+  w0 = 0;
+  w1 = l.cnt[col];
+  al = 0.0f;
+  if (!(g.vert_dist > 0.0)) return;
+  const int glat = col % g.num_lat + 1, glon = col / g.num_lat + 1;
+  const size_t ci = (size_t)(glat - 1 + g.halo) +
+                    (size_t)(g.num_lat + 2 * g.halo) * (size_t)(glon - 1 + g.halo);
+  const double aps = axb[g.ps_row + (size_t)g.n * ci];
+  auto lev = [&](int k1) {
+    if (g.vcoord == LG_VCOORD_SIGMA) return g.ca[k1 - 1] * (aps - g.ptop) + g.ptop;
+    return g.ca[k1 - 1] * (g.p0 - g.ptop) + g.cb[k1 - 1] * (aps - g.ptop) + g.ptop;
+  };
+  al = (float)log(0.5 * (lev(kk) + lev(kk + 1)));
+  const float span = 2.0f * (float)g.vert_dist;
+  int b_lo = (int)floorf((al - span - rec.lo) * rec.inv_dz) - 1;
+  int b_hi = (int)floorf((al + span - rec.lo) * rec.inv_dz) + 1;
+  b_lo = b_lo < 0 ? 0 : (b_lo > rec.nb - 1 ? rec.nb - 1 : b_lo);
+  b_hi = b_hi < 0 ? 0 : (b_hi > rec.nb - 1 ? rec.nb - 1 : b_hi);
+  const int* bo = rec.boff + (size_t)col * (rec.nb + 1);
+  w0 = bo[b_lo];
+  w1 = bo[b_hi + 1];
+}
+
+// work item -> column and its first level (1-based) and level count
+__device__ inline void item_levels(const SolveBatch& b, int item, int& col, int& kk0, int& G) {
+  const int ngrp = (b.levels + kG - 1) / kG;
+  col = b.first_col + item / ngrp;
+  kk0 = (item % ngrp) * kG + 1;
+  G = min(kG, b.levels - kk0 + 1);
+}
+
+}  // namespace colk
+
+__global__ void __launch_bounds__(colk::kThreads, 1)
+    gram_col_kernel(Geometry g, HxDev hx, ListDev l, SolveBatch b, const double* axb,
+                    double* Cout, double* tout, int* err, RecDev rec) {
+  using namespace colk;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t full[kRing], empty[kRing], ready[kOps], opdone[kOps], tmem_free;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ float s_t[4][64];
+  __shared__ volatile int s_abort;
+  __shared__ int s_go;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int k = g.ens;
+  const int ngrp = (b.levels + kG - 1) / kG;
+  const int nitems = b.ncols * ngrp;
+  const bool vertical = g.vert_dist > 0.0;
+  float* Y = reinterpret_cast<float*>(smem + kOffY);
+  unsigned char* ops = smem + kOffOps;
+  float4* R = reinterpret_cast<float4*>(smem + kOffRec);
+
+  if (tid == 0) {
+    for (int i = 0; i < kRing; ++i) {
+      tc::mbar_init(&full[i], 64);  // 32 record arrivals + 32 copy-completion arrivals
+      tc::mbar_init(&empty[i], 8);  // one per converter warp
+    }
+    for (int i = 0; i < kOps; ++i) {
+      tc::mbar_init(&ready[i], 8);  // one per converter warp
+      tc::mbar_init(&opdone[i], 1);  // tcgen05.commit
+    }
+    tc::mbar_init(&tmem_free, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_abort = 0;
+  }
+  // the Y ring starts at zero: members >= k are never copied and stay 0
+  for (int i = tid; i < kRing * kYBytes / 16; i += kThreads)
+    reinterpret_cast<uint4*>(smem + kOffY)[i] = make_uint4(0u, 0u, 0u, 0u);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc::smem_u32(&tmem_base_sh)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tmem_base_sh;
+
+  // lane 0 waits, the warp follows its outcome (keeps the warp converged)
+  auto wait_warp = [&](uint64_t* bar, int parity) {
+    int r = 0;
+    if (lane == 0) r = wait(bar, (uint32_t)(parity & 1), &s_abort) ? 1 : 0;
+    return __shfl_sync(0xffffffffu, r, 0) != 0;
+  };
+  // the item's levels: lane lv (< G) holds level lv's ln p and record window;
+  // [u0, u1) is the union of the windows.  Every role computes its own copy.
+  auto item_windows = [&](int item, int& col, int& kk0, int& G, float& al, int& w0, int& w1,
+                          int& u0, int& u1) {
+    item_levels(b, item, col, kk0, G);
+    al = 0.0f;
+    w0 = INT_MAX;
+    w1 = 0;
+    if (lane < G) level_window(g, l, rec, axb, col, kk0 + lane, al, w0, w1);
+    u0 = w0;
+    u1 = w1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      u0 = min(u0, __shfl_xor_sync(0xffffffffu, u0, o));
+      u1 = max(u1, __shfl_xor_sync(0xffffffffu, u1, o));
+    }
+  };
+
+  if (warp == kProducer) {
+    // ------------------------------------------------------------ producer
+    int pst = 0;
+    const int half = lane >> 4, part = lane & 15;
+    const int cpr = k >> 2;  // 16-byte chunks per ensemble row
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);  // weight 0: padding
+    bool ok = true;
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      int col, kk0, G, w0, w1, u0, u1;
+      float al;
+      item_windows(item, col, kk0, G, al, w0, w1, u0, u1);
+      if (u1 <= u0) continue;
+      const int64_t base = l.off[col];
+      const int nst = (u1 - u0 + kRows - 1) / kRows;
+      auto ldrec = [&](int st, float4& a, float4& c) {
+        const int i0 = u0 + st * kRows + lane, i1 = i0 + 32;
+        a = i0 < u1 ? rec.r[base + i0] : z4;
+        c = i1 < u1 ? rec.r[base + i1] : z4;
+      };
+      float4 r0, r1;
+      ldrec(0, r0, r1);
+      for (int st = 0; st < nst; ++st, ++pst) {
+        const int slot = pst % kRing;
+        if (pst >= kRing && !wait_warp(&empty[slot], pst / kRing - 1)) {
+          ok = false;
+          break;
+        }
+        float4* Rs = R + slot * kRows;
+        Rs[lane] = r0;
+        Rs[lane + 32] = r1;
+        arrive(&full[slot]);
+        __syncwarp();
+        if (st + 1 < nst) ldrec(st + 1, r0, r1);  // in flight while this stage's rows are issued
+        float* Ys = Y + (size_t)slot * kRows * 64;
+        for (int row = half; row < kRows; row += 2) {
+          const float4 rr = Rs[row];
+          if (part < cpr && rr.z > 0.0f)
+            cp_async16(Ys + row * 64 + part * 4,
+                       hx.yb32 + (size_t)__float_as_int(rr.x) * k + part * 4);
+        }
+        cp_async_arrive(&full[slot]);
+      }
+    }
+    cp_async_wait_all();
+  } else if (warp == kMmaWarp) {
+    // ------------------------------------------------------------ MMA issuer
+    int p = 0, mma_items = 0;  // items with at least one MMA so far
+    bool ok = true;
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      int col, kk0, G, w0, w1, u0, u1;
+      float al;
+      item_windows(item, col, kk0, G, al, w0, w1, u0, u1);
+      const int nst = u1 > u0 ? (u1 - u0 + kRows - 1) / kRows : 0;
+      unsigned started = 0u;
+      for (int st = 0; st < nst && ok; ++st) {
+        const int r0 = u0 + st * kRows;
+        for (int lv = 0; lv < kG; ++lv) {
+          const int lw0 = __shfl_sync(0xffffffffu, w0, lv), lw1 = __shfl_sync(0xffffffffu, w1, lv);
+          if (!(r0 + kRows > lw0 && r0 < lw1)) continue;
+          // before the item's first MMA: the previous MMA item's epilogue has
+          // copied its accumulators out of tensor memory
+          if (started == 0u && mma_items > 0 && !wait_warp(&tmem_free, mma_items - 1)) {
+            ok = false;
+            break;
+          }
+          const int buf = p % kOps;
+          if (!wait_warp(&ready[buf], p / kOps)) {
+            ok = false;
+            break;
+          }
+          if (lane == 0) {
+            tc::fence_after();
+            const uint32_t a0 = tc::smem_u32(ops + buf * kOpBytes);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              const uint64_t da = tc::make_desc(a0 + c * kChunkA, 128, 256);
+              mma(tmem + (uint32_t)(lv * kN), da, da, (((started >> lv) & 1u) || c > 0) ? 1u : 0u);
+            }
+            tc::mma_commit(&opdone[buf]);
+          }
+          __syncwarp();
+          started |= 1u << lv;
+          ++p;
+        }
+      }
+      if (started) ++mma_items;
+    }
+    // this warp's MMAs are complete before the tensor memory is freed
+    if (p > 0 && lane == 0) {
+      const int o = p - 1;
+      for (long long it = 0; it < tc::kSpinLimit; ++it)
+        if (tc::mbar_try_wait(&opdone[o % kOps], (uint32_t)((o / kOps) & 1))) break;
+    }
+  } else {
+    // ------------------------------------------------------------ converters
+    const int m = tid & 63, q = tid >> 6;  // member; quarter q owns record groups q, q + 4
+    const float inv_vd = vertical ? (float)(1.0 / g.vert_dist) : 0.0f;
+    float* SW = reinterpret_cast<float*>(smem + kOffW) + warp * (2 * kG * 16);  // [kG][16]
+    float* SD = SW + kG * 16;
+    int cst = 0, p = 0;
+    unsigned long long nnz = 0;  // non-zero (record, level) weights, counted by warps 0, 2, 4, 6
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+      int col, kk0, G, w0, w1, u0, u1;
+      float al;
+      item_windows(item, col, kk0, G, al, w0, w1, u0, u1);
+      const int nst = u1 > u0 ? (u1 - u0 + kRows - 1) / kRows : 0;
+      unsigned started = 0u;
+      float tacc[kG];
+#pragma unroll
+      for (int lv = 0; lv < kG; ++lv) tacc[lv] = 0.0f;
+      bool ok = true;
+      for (int st = 0; st < nst && ok; ++st, ++cst) {
+        const int slot = cst % kRing;
+        if (!wait_warp(&full[slot], cst / kRing)) {
+          ok = false;
+          break;
+        }
+        const int r0 = u0 + st * kRows;
+        const float4* Rs = R + slot * kRows;
+        {
+          // weights of this warp's 16 records (lane & 15) for every level (lane >> 4 + 2j)
+          const int r = lane & 15;
+          const int row = r < 8 ? q * 8 + r : (q + 4) * 8 + (r - 8);
+          const float4 rc = Rs[row];
+#pragma unroll
+          for (int j = 0; j < kG / 2; ++j) {
+            const int lv = (lane >> 4) + 2 * j;
+            const float lal = __shfl_sync(0xffffffffu, al, lv);
+            const int lw0 = __shfl_sync(0xffffffffu, w0, lv), lw1 = __shfl_sync(0xffffffffu, w1, lv);
+            float wt = rc.z, sw = 0.0f, sd = 0.0f;
+            if (wt > 0.0f && r0 + row >= lw0 && r0 + row < lw1) {
+              if (vertical) {
+                const float z = fabsf(lal - rc.y) * inv_vd;
+                wt *= g.gc_filter_vertical ? tc::schr2f(z) : (z > 2.0f ? 0.0f : 1.0f);
+              }
+              if (wt > 0.0f) {
+                sw = sqrtf(wt);
+                sd = rc.w * sw;
+              }
+            }
+            nnz += (sw > 0.0f && (warp & 1) == 0) ? 1u : 0u;
+            SW[lv * 16 + r] = sw;
+            SD[lv * 16 + r] = sd;
+          }
+        }
+        float y[16];
+        const float* Ys = Y + (size_t)slot * kRows * 64;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) y[h * 8 + jj] = Ys[((q + 4 * h) * 8 + jj) * 64 + m];
+        __syncwarp();
+        if (lane == 0) arrive(&empty[slot]);  // this warp has read the stage
+#pragma unroll
+        for (int lv = 0; lv < kG; ++lv) {
+          const int lw0 = __shfl_sync(0xffffffffu, w0, lv), lw1 = __shfl_sync(0xffffffffu, w1, lv);
+          if (!(r0 + kRows > lw0 && r0 < lw1)) continue;
+          const int buf = p % kOps;
+          if (p >= kOps && !wait_warp(&opdone[buf], p / kOps - 1)) {
+            ok = false;
+            break;
+          }
+          unsigned char* A = ops + buf * kOpBytes;
+          const float4* sw4 = reinterpret_cast<const float4*>(SW + lv * 16);
+          const float4* sd4 = reinterpret_cast<const float4*>(SD + lv * 16);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int gi = q + 4 * h;
+            // weights of the group's 8 records (0 for padding: the ring holds finite
+            // values there, and zeros for members >= k)
+            const float4 wa = sw4[2 * h], wb = sw4[2 * h + 1];
+            const float4 da = sd4[2 * h], db = sd4[2 * h + 1];
+            const float swv[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+            const float sdv[8] = {da.x, da.y, da.z, da.w, db.x, db.y, db.z, db.w};
+            uint32_t hi[4], lo[4];
+#pragma unroll
+            for (int jj = 0; jj < 8; jj += 2) {
+              const float v0 = y[h * 8 + jj] * swv[jj];
+              const float v1 = y[h * 8 + jj + 1] * swv[jj + 1];
+              tacc[lv] = fmaf(v0, sdv[jj], tacc[lv]);
+              tacc[lv] = fmaf(v1, sdv[jj + 1], tacc[lv]);
+              tc::split_bf16x2(v0, v1, hi[jj / 2], lo[jj / 2]);
+            }
+            const int chunk = gi >> 1, kc = gi & 1;
+            const int off_hi = (m >> 3) * 256 + kc * 128 + (m & 7) * 16;
+            const int mlo = m + 64;
+            const int off_lo = (mlo >> 3) * 256 + kc * 128 + (mlo & 7) * 16;
+            *reinterpret_cast<uint4*>(A + chunk * kChunkA + off_hi) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+            *reinterpret_cast<uint4*>(A + chunk * kChunkA + off_lo) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+          }
+          tc::fence_proxy_async();
+          __syncwarp();
+          if (lane == 0) arrive(&ready[buf]);
+          started |= 1u << lv;
+          ++p;
+        }
+      }
+      // item end: the eight converter warps meet here whatever happened above
+      if (ok && p > 0) ok = wait_warp(&opdone[(p - 1) % kOps], (p - 1) / kOps);
+      if (!ok) s_abort = 1;
+      conv_sync();
+      if (tid == 0) s_go = s_abort ? 0 : 1;
+      conv_sync();
+      if (!s_go) break;
+      tc::fence_after();
+      float* D = reinterpret_cast<float*>(ops);
+      const int levels = b.levels;
+      for (int lv = 0; lv < G; ++lv) {
+        const size_t s = (size_t)(col - b.first_col) * levels + (kk0 - 1 + lv);
+        double* C = Cout + s * k * k;
+        double* t = tout + s * k;
+        if (!((started >> lv) & 1u)) {
+          for (int i = tid; i < k * k; i += kConv) C[i] = 0.0;
+          for (int i = tid; i < k; i += kConv) t[i] = 0.0;
+          continue;
+        }
+        if (warp < 4) {
+#pragma unroll
+          for (int c0 = 0; c0 < kN; c0 += 16) {
+            float v[16];
+            tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(lv * kN + c0), v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) D[(warp * 32 + lane) * kDS + c0 + i] = v[i];
+          }
+        }
+        float tv = 0.0f;
+#pragma unroll
+        for (int u = 0; u < kG; ++u)
+          if (u == lv) tv = tacc[u];
+        s_t[q][m] = tv;
+        conv_sync();
+        for (int idx = tid; idx < k * k; idx += kConv) {
+          const int i = idx % k, j = idx / k;
+          C[idx] = (double)(D[i * kDS + j] + (D[(64 + i) * kDS + j] + D[(64 + j) * kDS + i]));
+        }
+        if (tid < k) t[tid] = (double)((s_t[0][tid] + s_t[1][tid]) + (s_t[2][tid] + s_t[3][tid]));
+        conv_sync();
+      }
+      tc::fence_before();
+      conv_sync();
+      if (tid == 0 && started) arrive(&tmem_free);  // only items that used tensor memory
+    }
+    if (b.work) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) nnz += __shfl_xor_sync(0xffffffffu, nnz, o);
+      if (lane == 0 && nnz) atomicAdd(b.work, nnz);
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  if (tid == 0 && s_abort) atomicExch(err, LG_ERR_TIMEOUT);
+}
+
+bool gram_col_supported(int ens) { return ens <= 64 && ens % 4 == 0; }
+
+void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
+                     const double* axb, double* C, double* t, int* err, const RecDev& rec,
+                     cudaStream_t stream) {
+  if (b.nsolves == 0) return;
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const int ngrp = (b.levels + colk::kG - 1) / colk::kG;
+  const int nitems = b.ncols * ngrp;
+  const int grid = std::min(nitems, sms);
+  cudaFuncSetAttribute(gram_col_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       colk::kSmemBytes);
+  gram_col_kernel<<<grid, colk::kThreads, colk::kSmemBytes, stream>>>(g, hx, l, b, axb, C, t,
+                                                                      err, rec);
+}
+
+}  // namespace lg

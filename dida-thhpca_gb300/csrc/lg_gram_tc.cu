@@ -10,7 +10,10 @@
 //   D = A B  (FP32 accumulator in tensor memory)
 //   C = D[0:64,0:64] + D[64:128,0:64] + D[64:128,0:64]^T     (hi hi + lo hi + hi lo)
 //   t = D[0:64,64] + D[0:64,65] + D[64:128,64]
-// The lo x lo and lo x dlo terms (relative 2^-16) are dropped.
+// The lo x lo and lo x dlo terms (relative 2^-16) are dropped.  The three
+// accumulator terms are summed in FP32 before the conversion to FP64: the two
+// small ones are 2^-8 of the first, so the sum's rounding (2^-24) stays below
+// the accumulation error of the tensor-core sums themselves.
 //
 // One CTA (4 warps) per solve.  Nonzero-weight entries are compacted into a
 // shared queue, 64 at a time they are scaled, split and written to one of two
@@ -25,118 +28,11 @@
 
 #include "lg_device.cuh"
 #include "lg_internal.h"
+#include "lg_tc.cuh"
 
 namespace lg {
 
-namespace tc {
 
-constexpr int kThreads = 128;
-constexpr int kStageEntries = 64;           // 4 MMAs of K = 16
-constexpr int kChunkA = 128 * 16 * 2;       // 4096 B: M=128 x K=16 bf16
-constexpr int kChunkB = 80 * 16 * 2;        // 2560 B: N=80 x K=16 bf16
-constexpr int kStageBytes = 4 * (kChunkA + kChunkB);  // 26624 B
-constexpr int kN = 80;
-constexpr int kDS = kN + 1;  // row stride of the accumulator copy in shared memory (odd: no bank conflicts)
-constexpr int kTmemCols = 128;
-constexpr int kQueueCap = kStageEntries + kThreads;
-constexpr long long kSpinLimit = 1ll << 24;  // ~1 s of polling
-
-__device__ inline uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-// shared-memory matrix descriptor: K-major, no swizzle
-__device__ inline uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
-  return d;                // base offset 0, layout type 0 (no swizzle)
-}
-
-// instruction descriptor: kind::f16, BF16 A/B, FP32 D, K-major A and B, M=128, N=80
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
-                            ((uint32_t)(128 >> 4) << 24);
-
-__device__ inline void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ inline bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// bounded wait; returns false on expiry
-__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long i = 0; i < kSpinLimit; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-
-__device__ inline void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(da), "l"(db), "r"(kIdesc), "r"(accumulate));
-}
-
-__device__ inline void mma_commit(uint64_t* bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(bar))
-      : "memory");
-}
-
-__device__ inline void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ inline void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ inline void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// 16 consecutive FP32 accumulator columns of this thread's lane
-__device__ inline void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ inline float schr2f(float ri) {
-  if (ri > 2.0f) return 0.0f;
-  if (ri > 1.0f) {
-    float rj = ri / 12.0f - 0.5f;
-    rj = rj * ri + 0.625f;
-    rj = rj * ri + 1.666667f;
-    return (rj * ri - 5.0f) * ri + 4.0f - 0.6666667f / ri;
-  }
-  if (ri > 0.0f) {
-    float rk = ri * ri;
-    float rj = (-0.25f * ri + 0.5f) * ri + 0.625f;
-    return (rj * ri - 1.666667f) * rk + 1.0f;
-  }
-  return 1.0f;
-}
-
-__device__ inline uint32_t pack_bf16(float a, float b) {
-  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-  return *reinterpret_cast<uint32_t*>(&h);
-}
-
-}  // namespace tc
 
 __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev hx, ListDev l,
                                                               SolveBatch b, const double* axb,
@@ -161,7 +57,7 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev
   int p = 0;
   int col = 0;
   bool vertical = false;
-  const bool use_rec = (b.mode == 0) && rec.ent != nullptr;
+  const bool use_rec = (b.mode == 0) && rec.r != nullptr;
   if (b.mode == 0) {
     col = b.first_col + s / b.levels;
     const int kk = s % b.levels + 1;
@@ -234,10 +130,11 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev
         int ent;
         float w;
         if (use_rec) {
-          ent = rec.ent[base + i];
-          w = rec.w[base + i];
+          const float4 rr = rec.r[base + i];
+          ent = __float_as_int(rr.x);
+          w = rr.z;
           if (vertical) {
-            const float z = fabsf(al - rec.lnp[base + i]) * inv_vd;
+            const float z = fabsf(al - rr.y) * inv_vd;
             w *= g.gc_filter_vertical ? schr2f(z) : (z > 2.0f ? 0.0f : 1.0f);
           }
         } else if (b.mode == 0) {
@@ -383,10 +280,10 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev
     __syncthreads();
     for (int idx = tid; idx < k * k; idx += kThreads) {
       const int i = idx % k, j = idx / k;
-      C[idx] = (double)D[i * kDS + j] + (double)D[(64 + i) * kDS + j] + (double)D[(64 + j) * kDS + i];
+      C[idx] = (double)(D[i * kDS + j] + (D[(64 + i) * kDS + j] + D[(64 + j) * kDS + i]));
     }
     for (int i = tid; i < k; i += kThreads)
-      t[i] = (double)D[i * kDS + 64] + (double)D[i * kDS + 65] + (double)D[(64 + i) * kDS + 64];
+      t[i] = (double)(D[i * kDS + 64] + (D[i * kDS + 65] + D[(64 + i) * kDS + 64]));
   }
   if (!ok && tid == 0) s_fail = 1;
   fence_before();
@@ -435,6 +332,7 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_stream_kernel(Geometry g
   __shared__ float r_d[3][kStageEntries];   // sqrt(weight) * innovation
   __shared__ float s_al;
   __shared__ int s_fail;
+  __shared__ unsigned s_nnz;
 
   const int s = blockIdx.x;
   const int k = g.ens;
@@ -445,6 +343,7 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_stream_kernel(Geometry g
   const bool vertical = g.vert_dist > 0.0;
   if (tid == 0) {
     s_fail = 0;
+    s_nnz = 0u;
     s_al = 0.0f;
     if (vertical) {
       const int glat = col % g.num_lat + 1, glon = col / g.num_lat + 1;
@@ -501,15 +400,17 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_stream_kernel(Geometry g
       int ent = 0;
       float sw = 0.0f, sd = 0.0f;
       if (i < w1) {
-        ent = rec.ent[base + i];
-        float w = rec.w[base + i];
+        const float4 rr = rec.r[base + i];
+        ent = __float_as_int(rr.x);
+        float w = rr.z;
         if (vertical) {
-          const float z = fabsf(al - rec.lnp[base + i]) * inv_vd;
+          const float z = fabsf(al - rr.y) * inv_vd;
           w *= g.gc_filter_vertical ? schr2f(z) : (z > 2.0f ? 0.0f : 1.0f);
         }
         if (w > 0.0f) {
           sw = sqrtf(w);
-          sd = (float)hx.dis[ent] * sw;
+          sd = rr.w * sw;
+          atomicAdd(&s_nnz, 1u);
         }
       }
       r_ent[buf][e] = ent;
@@ -558,10 +459,7 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_stream_kernel(Geometry g
       for (int jj = 0; jj < 8; jj += 2) {
         const float v0 = cur[j * 8 + jj] * r_s[rb][gi * 8 + jj];
         const float v1 = cur[j * 8 + jj + 1] * r_s[rb][gi * 8 + jj + 1];
-        __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
-        const float2 hf = __bfloat1622float2(h2);
-        hi[jj / 2] = *reinterpret_cast<uint32_t*>(&h2);
-        lo[jj / 2] = pack_bf16(v0 - hf.x, v1 - hf.y);
+        split_bf16x2(v0, v1, hi[jj / 2], lo[jj / 2]);
       }
       const int chunk = gi >> 1, kc = gi & 1;
       const int off_row = (m >> 3) * 256 + kc * 128 + (m & 7) * 16;
@@ -623,10 +521,10 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_stream_kernel(Geometry g
     __syncthreads();
     for (int idx = tid; idx < k * k; idx += kThreads) {
       const int i = idx % k, j = idx / k;
-      C[idx] = (double)D[i * kDS + j] + (double)D[(64 + i) * kDS + j] + (double)D[(64 + j) * kDS + i];
+      C[idx] = (double)(D[i * kDS + j] + (D[(64 + i) * kDS + j] + D[(64 + j) * kDS + i]));
     }
     for (int i = tid; i < k; i += kThreads)
-      t[i] = (double)D[i * kDS + 64] + (double)D[i * kDS + 65] + (double)D[(64 + i) * kDS + 64];
+      t[i] = (double)(D[i * kDS + 64] + (D[i * kDS + 65] + D[(64 + i) * kDS + 64]));
   }
   if (!ok && tid == 0) s_fail = 1;
   fence_before();
@@ -635,7 +533,7 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_stream_kernel(Geometry g
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d),
                  "r"(kTmemCols));
   if (s_fail && tid == 0) atomicExch(err, LG_ERR_TIMEOUT);
-  if (b.work && tid == 0) atomicAdd(b.work, (unsigned long long)nrec);
+  if (b.work && tid == 0 && s_nnz) atomicAdd(b.work, (unsigned long long)s_nnz);
 }
 
 void launch_gram_tc_stream(const Geometry& g, const HxDev& hx, const ListDev& l,

@@ -98,9 +98,7 @@ struct ListDev {
 
 // Per-column entry records grouped by ln p bucket (mixed-precision Gram input).
 struct RecDev {
-  const int* ent;     // list-sized
-  const float* lnp;   // list-sized
-  const float* w;     // list-sized: rdiaginv * rloc (FP32)
+  const float4* r;    // list-sized: (entry index bits, ln p, rdiaginv * rloc, innovation), FP32
   const int* boff;    // columns x (nb+1)
   int nb;
   float lo, inv_dz;
@@ -157,11 +155,15 @@ inline cudaError_t record_event(cudaEvent_t e, cudaStream_t st) {
              ? cudaEventRecordWithFlags(e, st, cudaEventRecordExternal)
              : cudaEventRecord(e, st);
 }
+bool gram_col_supported(int ens);
+void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
+                     const double* axb, double* C, double* t, int* err, const RecDev& rec,
+                     cudaStream_t stream);
 void launch_gram_tc_stream(const Geometry& g, const HxDev& hx, const ListDev& l,
                            const SolveBatch& b, const double* axb, double* C, double* t, int* err,
                            const RecDev& rec, cudaStream_t stream);
 void launch_records(int ncol, const ListDev& l, const HxDev& hx, float lo, float inv_dz, int nb,
-                    int* boff, int* rec_ent, float* rec_lnp, float* rec_w, cudaStream_t stream);
+                    int* boff, float4* rec, cudaStream_t stream);
 void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
                       const double* xb, const double* axb, double* xa, double* axa,
                       double* trans, double* wbar, int* eig_fail, cudaStream_t stream);
@@ -171,8 +173,8 @@ void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const 
                  const double* xb, const double* axb, double* xa, double* axa, double* tri,
                  double* lam, void* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
                  int* overflow_list, int* overflow_n, int* eig_fail, bool fp32_vectors,
-                 cudaStream_t stream, cudaEvent_t ev_after_tri = nullptr,
-                 cudaEvent_t ev_after_ql = nullptr);
+                 int ql_warps, int vec_warps, cudaStream_t stream,
+                 cudaEvent_t ev_after_tri = nullptr, cudaEvent_t ev_after_ql = nullptr);
 void launch_split_mean(int ens, int64_t npts_rows, const double* xb_in, double* xb, double* axb,
                        int* err, cudaStream_t stream);
 void launch_post(int ens, int n, int num_lat, int num_lon, int halo, double gamma1, double gamma2,

@@ -156,8 +156,7 @@ namespace lg {
 // whole list.  One warp per column; the ranking inside a bucket uses the lane
 // order, so the layout is deterministic.
 __global__ void __launch_bounds__(128) records_kernel(int ncol, ListDev l, HxDev hx, float lo,
-                                                      float inv_dz, int nb, int* boff, int* rec_ent,
-                                                      float* rec_lnp, float* rec_w) {
+                                                      float inv_dz, int nb, int* boff, float4* rec) {
   const int warps = blockDim.x / 32;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int col = blockIdx.x * warps + w;
@@ -205,9 +204,8 @@ __global__ void __launch_bounds__(128) records_kernel(int ncol, ListDev l, HxDev
     __syncwarp();
     if (ok) {
       const int64_t pos = base + start + rank;
-      rec_ent[pos] = ent;
-      rec_lnp[pos] = (float)hx.lnp[ent];
-      rec_w[pos] = hx.rdiag[ent] * (float)l.rloc[base + i];
+      rec[pos] = make_float4(__int_as_float(ent), (float)hx.lnp[ent],
+                             hx.rdiag[ent] * (float)l.rloc[base + i], (float)hx.dis[ent]);
     }
     if (ok && rank == 0) cur[b] = start + __popc(same);
     __syncwarp();
@@ -215,11 +213,11 @@ __global__ void __launch_bounds__(128) records_kernel(int ncol, ListDev l, HxDev
 }
 
 void launch_records(int ncol, const ListDev& l, const HxDev& hx, float lo, float inv_dz, int nb,
-                    int* boff, int* rec_ent, float* rec_lnp, float* rec_w, cudaStream_t stream) {
+                    int* boff, float4* rec, cudaStream_t stream) {
   const int warps = 4;
   const size_t smem = sizeof(int) * warps * (nb + 1);
   records_kernel<<<(ncol + warps - 1) / warps, 32 * warps, smem, stream>>>(
-      ncol, l, hx, lo, inv_dz, nb, boff, rec_ent, rec_lnp, rec_w);
+      ncol, l, hx, lo, inv_dz, nb, boff, rec);
 }
 
 }  // namespace lg

@@ -81,6 +81,19 @@ class LgStats(C.Structure):
 
 
 # ----------------------------------------------------------------- configs
+LG_GRAM_AUTO, LG_GRAM_COLUMN, LG_GRAM_STREAM, LG_GRAM_QUEUE = 0, 1, 2, 3
+
+
+class LgTuning(C.Structure):
+    """lg_tuning: launch shapes and bucket boundaries (lg_set_tuning / lg_autotune)."""
+    _fields_ = [("chunk_mb", C.c_int), ("gram_kernel", C.c_int), ("lnp_buckets", C.c_int),
+                ("ql_warps", C.c_int), ("vec_warps", C.c_int), ("solve_streams", C.c_int),
+                ("ms", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 @dataclasses.dataclass
 class Config:
     """Python view of lg_config plus the synthetic-workload description."""
@@ -274,6 +287,9 @@ def load_library(path: str = LIB_PATH):
     lib.lg_run_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p]
     lib.lg_get_stats.argtypes = [C.c_void_p, P(LgStats)]
+    lib.lg_get_tuning.argtypes = [C.c_void_p, P(LgTuning)]
+    lib.lg_set_tuning.argtypes = [C.c_void_p, P(LgTuning)]
+    lib.lg_autotune.argtypes = [C.c_void_p] + [C.c_void_p] * 5 + [P(LgTuning)]
     lib.lg_get_lists.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_double),
                                  P(C.c_int64)]
     lib.lg_copy_layout.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int64),
@@ -392,6 +408,27 @@ class Letkf:
                                           _ptr(xb_in, C.c_double), _ptr(xa_out, C.c_double),
                                           _ptr(spread_b, C.c_double), _ptr(spread_a, C.c_double)),
               "lg_run_da_parallel")
+
+    def tuning(self) -> dict:
+        t = LgTuning()
+        check(self.lib.lg_get_tuning(self.h, C.byref(t)), "lg_get_tuning")
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        t = LgTuning()
+        check(self.lib.lg_get_tuning(self.h, C.byref(t)), "lg_get_tuning")
+        for key, v in kw.items():
+            setattr(t, key, v)
+        check(self.lib.lg_set_tuning(self.h, C.byref(t)), "lg_set_tuning")
+
+    def autotune(self, xb, axb, xa, axa, stream=None) -> dict:
+        """lg_autotune on torch CUDA tensors; returns the chosen settings."""
+        t = LgTuning()
+        s = C.c_void_p(stream) if stream is not None else None
+        check(self.lib.lg_autotune(self.h, C.c_void_p(xb.data_ptr()), C.c_void_p(axb.data_ptr()),
+                                   C.c_void_p(xa.data_ptr()), C.c_void_p(axa.data_ptr()), s,
+                                   C.byref(t)), "lg_autotune")
+        return t.as_dict()
 
     def stats(self) -> dict:
         st = LgStats()

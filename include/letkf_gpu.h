@@ -193,6 +193,43 @@ int lg_run_da_parallel(lg_ctx* ctx, int ntimes, double gamma1, double gamma2, do
 /* Statistics of the last lg_run. */
 int lg_get_stats(const lg_ctx* ctx, lg_stats* st);
 
+/* Launch shapes and bucket boundaries of the analysis.  None of them changes
+ * an FP64 result; in mixed precision the Gram variant and the ln p buckets only
+ * change the FP32 summation order.  No reference counterpart: the reference
+ * has no GPU path to tune. */
+#define LG_GRAM_AUTO 0   /* column groups where supported, else per-solve streaming */
+#define LG_GRAM_COLUMN 1 /* one CTA per SM over (column, 8 levels) items, rows read once per group */
+#define LG_GRAM_STREAM 2 /* one CTA per solve streaming its ln p window of records */
+#define LG_GRAM_QUEUE 3  /* one CTA per solve compacting non-zero weights through a queue */
+
+typedef struct lg_tuning {
+  int chunk_mb;    /* Gram workspace per solve chunk [MiB] (sets solves per launch), 16..65536 */
+  int gram_kernel; /* LG_GRAM_* (mixed precision) */
+  int lnp_buckets; /* ln p buckets of the Gram records (mixed, vertical localisation), 8..1024:
+                      the bucket boundaries that bound each level's record window */
+  int ql_warps;    /* warps per block of the QL kernel, 1..6 */
+  int vec_warps;   /* warps per block of the vector/update kernel, 1..8 */
+  int solve_streams; /* 1, or 2: chunks alternate between two streams with their own
+                        scratch, so one chunk's Gram overlaps another's eigensolve */
+  double ms;       /* device time of one analysis with these settings (lg_autotune) */
+} lg_tuning;
+
+/* Current settings; defaults are the autotuned values of the 360x180x32, N=64,
+ * 10^6-observation workload. */
+int lg_get_tuning(const lg_ctx* ctx, lg_tuning* out);
+
+/* Apply settings (validated; LG_ERR_ARG if out of range).  Buffers are resized
+ * and the captured analysis graph is rebuilt at the next run. */
+int lg_set_tuning(lg_ctx* ctx, const lg_tuning* t);
+
+/* Autotuner: times complete analyses of the given device arrays (as
+ * lg_run_device) over candidate settings -- chunk size, Gram variant, ln p
+ * bucket count, QL and vector block shapes, solve streams -- one parameter at a time,
+ * applies the fastest and returns it in *best (best->ms = its analysis time).
+ * xa/axa are overwritten by the analyses. */
+int lg_autotune(lg_ctx* ctx, const double* d_xb, const double* d_axb, double* d_xa,
+                double* d_axa, void* stream, lg_tuning* best);
+
 /* Neighbour lists of the last analysis (device-built), for parity checks.
  * counts: num_lat*num_lon ints, column c = (lon-1)*num_lat + (lat-1);
  * entries/rloc: total local entries in column order; entries hold the global

@@ -18,7 +18,8 @@ def declared_functions():
 def test_header_declares_expected_entry_points():
     names = declared_functions()
     for n in ("lg_create", "lg_set_grid", "lg_set_obs", "lg_run", "lg_run_device",
-              "lg_core_batch", "letkf_core_", "lg_destroy", "lg_get_stats"):
+              "lg_core_batch", "letkf_core_", "lg_destroy", "lg_get_stats", "lg_get_tuning",
+              "lg_set_tuning", "lg_autotune"):
         assert n in names
 
 
@@ -42,6 +43,9 @@ def test_status_strings_and_null_arguments(built_lib):
     cfg.ens = 1
     assert L.lg_create(C.byref(h), C.byref(cfg)) == -1
     assert L.lg_letkf_core(1, 0, None, None, None, None, None, None, 1.0) == -1
+    assert L.lg_get_tuning(None, None) == -1
+    assert L.lg_set_tuning(None, None) == -1
+    assert L.lg_autotune(None, None, None, None, None, None, None) == -1
 
 
 def test_python_mirror_struct_layout_matches_header(built_lib, tmp_path):
@@ -51,7 +55,7 @@ def test_python_mirror_struct_layout_matches_header(built_lib, tmp_path):
 
     import letkf_gb300 as lg
     structs = {"lg_config": lg.LgConfig, "lg_obs_type": lg.LgObsType,
-               "lg_obs_soa": lg.LgObsSoa, "lg_stats": lg.LgStats}
+               "lg_obs_soa": lg.LgObsSoa, "lg_stats": lg.LgStats, "lg_tuning": lg.LgTuning}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "letkf_gpu.h"',
              "int main(void) {"]
     for cname, py in structs.items():

@@ -91,3 +91,37 @@ def test_mixed_analysis_increment_within_1e4(name, over):
     off = np.concatenate([[0], np.cumsum(counts)])
     assert np.array_equal(ent[off[5]:off[6]], e_o)
     ctx.letkf_final()
+
+
+@pytest.mark.parametrize("name", ["small3d", "tiny2d"])
+def test_tensor_core_gram_variants_agree(name, monkeypatch):
+    """The column-group Gram (default), the per-solve streaming Gram and the
+    per-solve compaction-queue Gram all meet the increment tolerance and agree
+    with one another far inside it (tiny2d has no vertical localisation: one
+    level per column)."""
+    import letkf_gb300 as lg
+    import synth
+    from oracle import oracle as orc
+
+    cfg = lg.preset(name).replace(precision=lg.LG_PREC_MIXED)
+    w = synth.make_workload(cfg)
+    o = orc.Oracle(cfg, w.obs)
+    o.hx(w.xb, w.axb)
+    xa_o = np.zeros_like(w.xb)
+    axa_o = np.zeros_like(w.axb)
+    o.analysis(w.xb, w.axb, xa_o, axa_o)
+    got = {}
+    for kind in ("col", "stream", "queue"):
+        monkeypatch.setenv("LETKF_GB300_GRAM", kind)
+        ctx = lg.Letkf(cfg)
+        ctx.set_obs(w.obs)
+        xa = np.zeros_like(w.xb)
+        axa = np.zeros_like(w.axb)
+        ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+        ctx.letkf_final()
+        errs = increment_rel_rms(cfg, w, (xa, axa), (xa_o, axa_o))
+        assert max(errs.values()) <= TOL_INCREMENT, (kind, errs)
+        got[kind] = (xa, axa)
+    for kind in ("stream", "queue"):
+        errs = increment_rel_rms(cfg, w, got[kind], got["col"])
+        assert max(errs.values()) <= 1e-5, (kind, errs)

@@ -1,0 +1,87 @@
+"""GPU tests of the launch-shape settings and the autotuner (lg_set_tuning,
+lg_autotune): settings are validated, no setting changes an FP64 analysis by a
+single bit, and the autotuned mixed-precision analysis stays within the
+increment tolerance of the FP64 oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _workload(name, **over):
+    import letkf_gb300 as lg
+    import synth
+    cfg = lg.preset(name).replace(**over)
+    return cfg, synth.make_workload(cfg)
+
+
+def _device_run(ctx, w):
+    import torch
+    dev = torch.device("cuda")
+    xb = torch.as_tensor(w.xb, device=dev)
+    axb = torch.as_tensor(w.axb, device=dev)
+    xa = torch.zeros_like(xb)
+    axa = torch.zeros_like(axb)
+    return xb, axb, xa, axa
+
+
+def test_set_tuning_validates_and_round_trips():
+    import letkf_gb300 as lg
+    cfg, w = _workload("tiny3d")
+    ctx = lg.Letkf(cfg)
+    t = ctx.tuning()
+    assert t["chunk_mb"] >= 16 and t["ql_warps"] >= 1 and t["vec_warps"] >= 1
+    ctx.set_tuning(chunk_mb=64, ql_warps=2, vec_warps=8, lnp_buckets=32)
+    t2 = ctx.tuning()
+    assert (t2["chunk_mb"], t2["ql_warps"], t2["vec_warps"], t2["lnp_buckets"]) == (64, 2, 8, 32)
+    for bad in ({"chunk_mb": 1}, {"ql_warps": 0}, {"ql_warps": 7}, {"vec_warps": 9},
+                {"lnp_buckets": 4}, {"gram_kernel": 9}, {"solve_streams": 3}):
+        with pytest.raises(RuntimeError, match="LG_ERR_ARG"):
+            ctx.set_tuning(**bad)
+    ctx.letkf_final()
+
+
+def test_fp64_analysis_is_bit_identical_under_every_setting():
+    import letkf_gb300 as lg
+    cfg, w = _workload("tiny3d")
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    ref = None
+    for kw in ({}, {"chunk_mb": 16}, {"ql_warps": 4, "vec_warps": 2}, {"vec_warps": 8},
+               {"solve_streams": 2, "chunk_mb": 16}):
+        ctx.set_tuning(**kw)
+        xa = np.zeros_like(w.xb)
+        axa = np.zeros_like(w.axb)
+        ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+        if ref is None:
+            ref = (xa, axa)
+        else:
+            assert np.array_equal(xa, ref[0]) and np.array_equal(axa, ref[1]), kw
+    ctx.letkf_final()
+
+
+def test_autotune_mixed_keeps_the_increment_within_tolerance():
+    import letkf_gb300 as lg
+    from oracle import oracle as orc
+    from test_gpu_mixed import TOL_INCREMENT, increment_rel_rms
+    cfg, w = _workload("small3d", precision=lg.LG_PREC_MIXED)
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    xb, axb, xa, axa = _device_run(ctx, w)
+    best = ctx.autotune(xb, axb, xa, axa)
+    assert best["ms"] > 0.0
+    assert best["gram_kernel"] in (lg.LG_GRAM_COLUMN, lg.LG_GRAM_STREAM, lg.LG_GRAM_QUEUE)
+    assert ctx.tuning()["chunk_mb"] == best["chunk_mb"]
+    ctx.letkf_run_device(0, xb, axb, xa, axa)
+    import torch
+    torch.cuda.synchronize()
+    o = orc.Oracle(cfg, w.obs)
+    o.hx(w.xb, w.axb)
+    xa_o = np.zeros_like(w.xb)
+    axa_o = np.zeros_like(w.axb)
+    o.analysis(w.xb, w.axb, xa_o, axa_o)
+    errs = increment_rel_rms(cfg, w, (xa.cpu().numpy(), axa.cpu().numpy()), (xa_o, axa_o))
+    assert max(errs.values()) <= TOL_INCREMENT, (best, errs)
+    ctx.letkf_final()

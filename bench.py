@@ -37,6 +37,13 @@ for p in (ROOT, PKG):
 
 METRIC = "LETKF grid columns/s, mixed vs plain FP64 on one GB300 at <=1e-4 rel RMS"
 UNIT = "columns/s"
+# DRAM bytes (read + write) per solve of the solve-phase kernels, from an ncu
+# capture of the 180x90x32 / N=64 / 2.5e5-observation workload in 256 MiB
+# chunks (8192 solves per launch; profiles/traffic_solve_kernels_prof.md).
+PROFILED_DRAM_BYTES_PER_SOLVE = {
+    "tridiag": 31.8e3,
+    "gram": 29.6e3,
+}
 
 
 def parse():
@@ -279,26 +286,38 @@ def main():
     value = world * ncol / (ms * 1e-3)
     st = ctx.stats()
 
-    # roofline of the dominant kernel: algorithmic FLOPs of all its launches in
-    # the timed steps over the sum of their event-timed durations
+    # Per-kernel durations without overlap: one more analysis on a single solve
+    # stream (outside the timed region) gives every kernel its own event time;
+    # in the timed two-stream configuration the Gram of one chunk runs beside the
+    # eigensolve of another, so per-phase stream times overlap.
+    if tuning["solve_streams"] != 1:
+        ctx.set_tuning(solve_streams=1)
+        step()
+    step()
+    torch.cuda.synchronize()
+    iso = ctx.stats()
+    if tuning["solve_streams"] != 1:
+        ctx.set_tuning(solve_streams=tuning["solve_streams"])
+
+    # roofline of the dominant kernel: algorithmic FLOPs of its launches in one
+    # analysis over the sum of their event-timed durations
     peaks = measured_peaks()
     k = cfg.ens
-    solves = st["n_solves"] * args.steps
+    solves = iso["n_solves"]
     fp64_peak = fp64_peak_tflops(torch, dev)
     mixed = cfg.precision == lg.LG_PREC_MIXED
     kernels = {
-        # 2 p k^2 (Gram, SURVEY convention) + 2 p k (Yb^T R^-1 d) over non-zero-weight entries
-        "gram": {"ms": acc["ms_gram"], "bound": "tensor" if mixed else "fp64",
-                 "flops": 2.0 * acc["n_gram_entries"] * k * k + 2.0 * acc["n_gram_entries"] * k},
+        # 2 p k^2 (Gram) + 2 p k (Yb^T R^-1 d) over the non-zero-weight (entry, level) pairs
+        "gram": {"ms": iso["ms_gram"], "bound": "tensor" if mixed else "fp64",
+                 "flops": 2.0 * iso["n_gram_entries"] * k * k + 2.0 * iso["n_gram_entries"] * k},
         # Householder tridiagonalisation of a symmetric k x k matrix: 4k^3/3
-        "tridiag": {"ms": acc["ms_tridiag"], "bound": "fp64", "flops": solves * 4.0 * k ** 3 / 3.0},
-        "ql": {"ms": acc["ms_ql"], "bound": "fp64", "flops": None},
-        "vec_update": {"ms": acc["ms_vec"], "bound": "fp32" if mixed else "fp64", "flops": None},
-        "search": {"ms": acc["ms_search"], "bound": "fp32/l2", "flops": None},
-        "hx": {"ms": acc["ms_hx"], "bound": "hbm", "flops": None},
+        "tridiag": {"ms": iso["ms_tridiag"], "bound": "fp64", "flops": solves * 4.0 * k ** 3 / 3.0},
+        "ql": {"ms": iso["ms_ql"], "bound": "fp64", "flops": None},
+        "vec_update": {"ms": iso["ms_vec"], "bound": "fp32" if mixed else "fp64", "flops": None},
+        "search": {"ms": iso["ms_search"], "bound": "fp32/l2", "flops": None},
+        "hx": {"ms": iso["ms_hx"], "bound": "hbm", "flops": None},
     }
     for name, kk in kernels.items():
-        kk["ms_per_step"] = kk["ms"] / args.steps
         if kk["flops"] and kk["ms"] > 0:
             kk["achieved_tflops"] = kk["flops"] / (kk["ms"] * 1e-3) / 1e12
     dom_name = max((n for n in kernels if kernels[n]["flops"]), key=lambda n: kernels[n]["ms"])
@@ -308,12 +327,16 @@ def main():
     else:
         peak, peak_src = fp64_peak, "cuBLAS DGEMM measured in this run (FP64 is not in MEASURED_PEAKS.json)"
     achieved = dom.get("achieved_tflops", 0.0)
-    launches_dom = max(1, acc["n_chunks"])
+    launches_dom = max(1, iso["n_chunks"])
+    traffic = None
+    if dom_name in PROFILED_DRAM_BYTES_PER_SOLVE:
+        traffic = PROFILED_DRAM_BYTES_PER_SOLVE[dom_name] * solves / launches_dom
     roofline = {"bound": dom["bound"], "kernel": dom_name, "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": traffic,
+                "traffic_note": "DRAM bytes per launch: ncu per-solve figure (profiles/) x solves per launch",
                 "peak_source": peak_src, "launches": launches_dom,
                 "ms_per_launch": dom["ms"] / launches_dom,
-                "share_of_step": dom["ms"] / (ms * args.steps)}
+                "share_of_single_stream_step": dom["ms"] / iso["ms_total"] if iso["ms_total"] else None}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -332,7 +355,8 @@ def main():
                    "tuning": {kk: v for kk, v in tuning.items() if kk != "ms"}},
         "clocks": clocks,
         "gpu_launches": acc["n_launches"],
-        "phases_ms": {n: round(v["ms_per_step"], 3) for n, v in kernels.items()},
+        "phases_ms": {n: round(v["ms"], 3) for n, v in kernels.items()},
+        "phases_note": "kernel event times of one single-stream analysis (no overlap)",
         "kernels": {n: {kk: v[kk] for kk in ("bound", "achieved_tflops") if kk in v}
                     for n, v in kernels.items()},
         "roofline": roofline,

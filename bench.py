@@ -307,9 +307,11 @@ def main():
     fp64_peak = fp64_peak_tflops(torch, dev)
     mixed = cfg.precision == lg.LG_PREC_MIXED
     kernels = {
-        # 2 p k^2 (Gram) + 2 p k (Yb^T R^-1 d) over the non-zero-weight (entry, level) pairs
+        # symmetric Gram p k (k+1) + Yb^T R^-1 d 2 p k, over the non-zero-weight
+        # (entry, level) pairs: the flops the product needs, counting each
+        # off-diagonal pair once (the FP64 kernel computes one triangle)
         "gram": {"ms": iso["ms_gram"], "bound": "tensor" if mixed else "fp64",
-                 "flops": 2.0 * iso["n_gram_entries"] * k * k + 2.0 * iso["n_gram_entries"] * k},
+                 "flops": 1.0 * iso["n_gram_entries"] * k * (k + 1) + 2.0 * iso["n_gram_entries"] * k},
         # Householder tridiagonalisation of a symmetric k x k matrix: 4k^3/3
         "tridiag": {"ms": iso["ms_tridiag"], "bound": "fp64", "flops": solves * 4.0 * k ** 3 / 3.0},
         "ql": {"ms": iso["ms_ql"], "bound": "fp64", "flops": None},
@@ -349,7 +351,8 @@ def main():
                                f"vert {cfg.vert_dist:g} ln p, rho={cfg.inflation}",
                    "precision": "mixed" if cfg.precision == lg.LG_PREC_MIXED else "fp64",
                    "columns": ncol, "solves_per_step": st["n_solves"],
-                   "local_entries_per_step": st["nobsl_total"],
+                   "list_entries_per_step": st["nobsl_total"],
+                   "gram_entries_per_step": iso["n_gram_entries"],
                    "l2": "inputs (background 3.4 GB) larger than L2; no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "tuning": {kk: v for kk, v in tuning.items() if kk != "ms"}},

@@ -71,10 +71,12 @@ struct lg_ctx {
     size_t cap = 0;        // solves
     size_t rot_n_cap = 0;  // rotation-log entries per solve it was sized for
   };
-  SolveLane lane[2];
+  SolveLane lane[3];
   int rot_cap = 0;
-  cudaStream_t side_stream = nullptr;  // second solve stream (tune.solve_streams = 2)
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // extra solve streams (tune.solve_streams 2 and 3) and their ordering events
+  cudaStream_t side_stream = nullptr, third_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join3 = nullptr;
+  cudaEvent_t ev_phase[3][3] = {};  // [Gram, eigensolve, vectors done][buffer set]
   // ln p bucketed records for the mixed-precision Gram
   float4* d_rec = nullptr;
   int* d_boff = nullptr;
@@ -83,7 +85,7 @@ struct lg_ctx {
   double lnp_span = 1.0;
   int boff_nb = 0;  // bucket count d_boff was sized for
   // launch shapes and bucket boundaries (lg_set_tuning / lg_autotune)
-  lg_tuning tune{1024, LG_GRAM_AUTO, 128, 1, 4, 2, 0.0};
+  lg_tuning tune{1024, LG_GRAM_AUTO, 128, 1, 4, 3, 0.0};
   // status words: [0] err, [1] eig_fail
   int* d_status = nullptr;
   unsigned long long* d_band = nullptr;
@@ -249,6 +251,25 @@ double box_bound(float v) {
   return strtod(buf, nullptr);
 }
 
+void release_streams(lg_ctx* c) {
+  for (cudaStream_t* sp : {&c->own_stream, &c->side_stream, &c->third_stream})
+    if (*sp) {
+      cudaStreamDestroy(*sp);
+      *sp = nullptr;
+    }
+  for (cudaEvent_t* ep : {&c->ev_fork, &c->ev_join, &c->ev_join3})
+    if (*ep) {
+      cudaEventDestroy(*ep);
+      *ep = nullptr;
+    }
+  for (auto& row : c->ev_phase)
+    for (auto& e : row)
+      if (e) {
+        cudaEventDestroy(e);
+        e = nullptr;
+      }
+}
+
 void drop_graph(lg_ctx* c) {
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   c->graph_exec = nullptr;
@@ -339,15 +360,18 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   lg_ctx* c = new lg_ctx();
   c->cfg = g;
   cudaGetDevice(&c->dev);
-  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
-    if (c->own_stream) cudaStreamDestroy(c->own_stream);
-  if (c->side_stream) cudaStreamDestroy(c->side_stream);
-  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-  if (c->ev_join) cudaEventDestroy(c->ev_join);
-    if (c->side_stream) cudaStreamDestroy(c->side_stream);
+  bool made = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&c->third_stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&c->ev_join3, cudaEventDisableTiming) == cudaSuccess;
+  for (auto& row : c->ev_phase)
+    for (auto& e : row)
+      made = made && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  if (!made) {
+    cudaGetLastError();
+    release_streams(c);
     delete c;
     return LG_ERR_CUDA;
   }
@@ -690,7 +714,7 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
 
 namespace {
 
-enum class GramKind { kColumn, kStream, kQueue };
+enum class GramKind { kColumn, kColumnLean, kStream, kQueue };
 
 // Timing events of an analysis go through lg::record_event (lg_internal.h), which
 // keeps them valid inside a CUDA-graph capture.
@@ -771,7 +795,7 @@ int prepare_capacity(lg_ctx* c) {
   // test hook: a small log forces the overflow fallback path
   if (const char* env = getenv("LETKF_GB300_ROT_CAP")) c->rot_cap = std::max(1, atoi(env));
   const int nl = c->tune.solve_streams;
-  for (int li = 0; li < 2; ++li) {
+  for (int li = 0; li < 3; ++li) {
     lg_ctx::SolveLane& L = c->lane[li];
     const size_t cap = li < nl ? (size_t)c->chunk * levels : 0;
     if (L.cap >= cap && (cap > 0 || L.cap == 0) && L.rot_n_cap == (size_t)c->rot_cap) continue;
@@ -797,7 +821,7 @@ int prepare_capacity(lg_ctx* c) {
     L.rot_n_cap = (size_t)c->rot_cap;
   }
   const int nchunks = (ncol + c->chunk - 1) / c->chunk;
-  while ((int)c->kev.size() < 5 * nchunks) {
+  while ((int)c->kev.size() < 7 * nchunks) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
     c->kev.push_back(e);
@@ -854,26 +878,49 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   const int levels = g.vert_dist > 0.0 ? g.nz : 1;
   const int chunk = c->chunk;
   const int nchunks = (ncol + chunk - 1) / chunk;
-  // tensor-core Gram variant: column groups (default), one CTA per solve
-  // streaming its records, or one CTA per solve with a compaction queue
-  GramKind gram_kind = lg::gram_col_supported(k) ? GramKind::kColumn : GramKind::kStream;
+  // tensor-core Gram variant.  Auto: the lean column Gram beside the phase
+  // pipeline's other streams, the full-size one otherwise; per-solve streaming
+  // where the column kernel does not apply.
+  GramKind gram_kind = !lg::gram_col_supported(k)       ? GramKind::kStream
+                       : c->tune.solve_streams == 3 ? GramKind::kColumnLean
+                                                    : GramKind::kColumn;
+  if (c->tune.gram_kernel == LG_GRAM_COLUMN && lg::gram_col_supported(k))
+    gram_kind = GramKind::kColumn;
+  if (c->tune.gram_kernel == LG_GRAM_COLUMN_LEAN && lg::gram_col_supported(k))
+    gram_kind = GramKind::kColumnLean;
   if (c->tune.gram_kernel == LG_GRAM_STREAM) gram_kind = GramKind::kStream;
   if (c->tune.gram_kernel == LG_GRAM_QUEUE) gram_kind = GramKind::kQueue;
   if (const char* e = getenv("LETKF_GB300_GRAM")) {
+    if (!strcmp(e, "col") && lg::gram_col_supported(k)) gram_kind = GramKind::kColumn;
+    if (!strcmp(e, "lean") && lg::gram_col_supported(k)) gram_kind = GramKind::kColumnLean;
     if (!strcmp(e, "stream")) gram_kind = GramKind::kStream;
     if (!strcmp(e, "queue")) gram_kind = GramKind::kQueue;
   }
-  // chunks alternate between the solve streams; each stream reuses its own
-  // scratch, so the Gram of one chunk can run beside the eigensolve of another
+  // Solve schedule over chunks of columns (tune.solve_streams):
+  //   1: every chunk on st;
+  //   2: chunks alternate between st and a second stream, each with its own
+  //      scratch, so the Gram of one chunk runs beside the eigensolve of another;
+  //   3: a phase pipeline over three buffer sets -- Grams on one stream,
+  //      tridiagonalisation + QL on st, vectors/update on a third, ordered by
+  //      events -- so the FP64 eigensolve of chunk q runs beside the Gram of
+  //      chunk q+1 and the vector update of chunk q-1.
+  // Per-chunk timing events (7 per chunk, each on its phase's stream): [0] Gram
+  // start, [1] Gram end, [2] eigensolve start, [3] after tridiag, [4] after QL,
+  // [5] vectors start, [6] vectors end.
   const int nl = c->tune.solve_streams;
-  cudaStream_t ss[2] = {st, c->side_stream};
-  if (nl == 2) {
+  if (nl >= 2) {
     CK(cudaEventRecord(c->ev_fork, st));
     CK(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
+    if (nl == 3) CK(cudaStreamWaitEvent(c->third_stream, c->ev_fork, 0));
   }
+  const bool fp32_vec = g.precision == LG_PREC_MIXED;
   for (int q = 0; q < nchunks; ++q) {
-    lg_ctx::SolveLane& L = c->lane[q % nl];
-    cudaStream_t s = ss[q % nl];
+    const int set = q % nl;
+    lg_ctx::SolveLane& L = c->lane[set];
+    cudaStream_t s = (nl == 2 && (q & 1)) ? c->side_stream : st;
+    cudaStream_t s_g = nl == 3 ? c->side_stream : s, s_e = s;
+    cudaStream_t s_v = nl == 3 ? c->third_stream : s;
+    cudaEvent_t* kv = &c->kev[7 * q];
     lg::SolveBatch b{};
     b.mode = 0;
     b.first_col = q * chunk;
@@ -881,42 +928,68 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     b.levels = levels;
     b.nsolves = b.ncols * levels;
     b.work = c->d_work;
-    CK(record_event(c->kev[5 * q], s));
-    if (mixed_tc && gram_kind == GramKind::kColumn)
-      lg::launch_gram_col(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec, s);
+    // Gram (phase pipeline: after the buffer set's previous vector update)
+    if (nl == 3 && q >= 3) CK(cudaStreamWaitEvent(s_g, c->ev_phase[2][set], 0));
+    CK(record_event(kv[0], s_g));
+    if (mixed_tc && (gram_kind == GramKind::kColumn || gram_kind == GramKind::kColumnLean))
+      lg::launch_gram_col(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec,
+                          gram_kind == GramKind::kColumnLean, s_g);
     else if (mixed_tc && gram_kind == GramKind::kStream)
-      lg::launch_gram_tc_stream(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec, s);
+      lg::launch_gram_tc_stream(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec, s_g);
     else if (mixed_tc)
-      lg::launch_gram_tc(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, s, &rec);
+      lg::launch_gram_tc(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, s_g, &rec);
     else
-      lg::launch_gram64(geo, c->hx, c->lists, b, axb, L.C, L.t, s);
-    CK(cudaMemsetAsync(L.ovf_n, 0, sizeof(int), s));
-    CK(record_event(c->kev[5 * q + 1], s));
+      lg::launch_gram64(geo, c->hx, c->lists, b, axb, L.C, L.t, s_g);
+    CK(cudaMemsetAsync(L.ovf_n, 0, sizeof(int), s_g));
+    CK(record_event(kv[1], s_g));
+    if (nl == 3) {
+      CK(cudaEventRecord(c->ev_phase[0][set], s_g));
+      CK(cudaStreamWaitEvent(s_e, c->ev_phase[0][set], 0));
+    }
+    CK(record_event(kv[2], s_e));
     if (c->use_eig2) {
       lg::launch_eig2(geo, b, L.C, L.t, xb, axb, xa, axa, L.tri, L.lam, L.rot_cs, L.rot_i,
-                      L.rot_n, c->rot_cap, L.ovf_list, L.ovf_n, c->d_status + 1,
-                      g.precision == LG_PREC_MIXED, c->tune.ql_warps, c->tune.vec_warps, s,
-                      c->kev[5 * q + 2], c->kev[5 * q + 3]);
+                      L.rot_n, c->rot_cap, L.ovf_list, L.ovf_n, c->d_status + 1, fp32_vec,
+                      c->tune.ql_warps, c->tune.vec_warps, lg::kEigTridiag | lg::kEigQL, s_e,
+                      kv[3], kv[4]);
+      if (nl == 3) {
+        CK(cudaEventRecord(c->ev_phase[1][set], s_e));
+        CK(cudaStreamWaitEvent(s_v, c->ev_phase[1][set], 0));
+      }
+      CK(record_event(kv[5], s_v));
+      lg::launch_eig2(geo, b, L.C, L.t, xb, axb, xa, axa, L.tri, L.lam, L.rot_cs, L.rot_i,
+                      L.rot_n, c->rot_cap, L.ovf_list, L.ovf_n, c->d_status + 1, fp32_vec,
+                      c->tune.ql_warps, c->tune.vec_warps, lg::kEigVectors, s_v);
       // matrices whose rotation log overflowed: accumulate-eigenvector solver
       lg::SolveBatch fb = b;
       fb.solve_list = L.ovf_list;
       fb.solve_count = L.ovf_n;
       lg::launch_eig_apply(geo, fb, L.C, L.t, xb, axb, xa, axa, nullptr, nullptr,
-                           c->d_status + 1, s);
+                           c->d_status + 1, s_v);
       launches += 4;
     } else {
       lg::launch_eig_apply(geo, b, L.C, L.t, xb, axb, xa, axa, nullptr, nullptr,
-                           c->d_status + 1, s);
-      CK(record_event(c->kev[5 * q + 2], s));
-      CK(record_event(c->kev[5 * q + 3], s));
+                           c->d_status + 1, s_e);
+      CK(record_event(kv[3], s_e));
+      CK(record_event(kv[4], s_e));
+      if (nl == 3) {
+        CK(cudaEventRecord(c->ev_phase[1][set], s_e));
+        CK(cudaStreamWaitEvent(s_v, c->ev_phase[1][set], 0));
+      }
+      CK(record_event(kv[5], s_v));
       launches += 1;
     }
-    CK(record_event(c->kev[5 * q + 4], s));
+    CK(record_event(kv[6], s_v));
+    if (nl == 3) CK(cudaEventRecord(c->ev_phase[2][set], s_v));
     launches += 1;
   }
-  if (nl == 2) {
+  if (nl >= 2) {
     CK(cudaEventRecord(c->ev_join, c->side_stream));
     CK(cudaStreamWaitEvent(st, c->ev_join, 0));
+    if (nl == 3) {
+      CK(cudaEventRecord(c->ev_join3, c->third_stream));
+      CK(cudaStreamWaitEvent(st, c->ev_join3, 0));
+    }
   }
   CK(record_event(c->ev[3], st));
   CK(cudaGetLastError());
@@ -982,10 +1055,11 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   CK(cudaStreamSynchronize(st));
   const int nchunks = (ncol + c->chunk - 1) / c->chunk;
   for (int q = 0; q < nchunks; ++q) {
-    const float a = elapsed_ms(c->kev[5 * q], c->kev[5 * q + 1]);
-    const float t1 = elapsed_ms(c->kev[5 * q + 1], c->kev[5 * q + 2]);
-    const float t2 = elapsed_ms(c->kev[5 * q + 2], c->kev[5 * q + 3]);
-    const float t3 = elapsed_ms(c->kev[5 * q + 3], c->kev[5 * q + 4]);
+    const cudaEvent_t* kv = &c->kev[7 * q];
+    const float a = elapsed_ms(kv[0], kv[1]);
+    const float t1 = elapsed_ms(kv[2], kv[3]);
+    const float t2 = elapsed_ms(kv[3], kv[4]);
+    const float t3 = elapsed_ms(kv[5], kv[6]);
     S.ms_gram += a;
     S.ms_tridiag += t1;
     S.ms_ql += t2;
@@ -1128,9 +1202,9 @@ int lg_get_tuning(const lg_ctx* c, lg_tuning* out) {
 int lg_set_tuning(lg_ctx* c, const lg_tuning* t) {
   if (!c || !t) return LG_ERR_ARG;
   if (t->chunk_mb < 16 || t->chunk_mb > 65536 || t->gram_kernel < LG_GRAM_AUTO ||
-      t->gram_kernel > LG_GRAM_QUEUE || t->lnp_buckets < 8 || t->lnp_buckets > 1024 ||
+      t->gram_kernel > LG_GRAM_COLUMN_LEAN || t->lnp_buckets < 8 || t->lnp_buckets > 1024 ||
       t->ql_warps < 1 || t->ql_warps > 6 || t->vec_warps < 1 || t->vec_warps > 8 ||
-      t->solve_streams < 1 || t->solve_streams > 2)
+      t->solve_streams < 1 || t->solve_streams > 3)
     return LG_ERR_ARG;
   c->tune = *t;
   c->capacity_ready = false;  // chunk size and bucket count size buffers
@@ -1147,7 +1221,9 @@ int lg_autotune(lg_ctx* c, const double* xb, const double* axb, double* xa, doub
   const bool vertical = g.vert_dist > 0.0;
   lg_tuning cur = c->tune;
   if (cur.gram_kernel == LG_GRAM_AUTO)
-    cur.gram_kernel = lg::gram_col_supported(g.ens) ? LG_GRAM_COLUMN : LG_GRAM_STREAM;
+    cur.gram_kernel = !lg::gram_col_supported(g.ens) ? LG_GRAM_STREAM
+                      : cur.solve_streams == 3          ? LG_GRAM_COLUMN_LEAN
+                                                        : LG_GRAM_COLUMN;
   // one untimed analysis (buffer sizing, graph capture), then the faster of two
   auto measure = [&](const lg_tuning& t, double* ms) -> int {
     int r = lg_set_tuning(c, &t);
@@ -1183,10 +1259,12 @@ int lg_autotune(lg_ctx* c, const double* xb, const double* axb, double* xa, doub
     }
     return LG_OK;
   };
+  if ((r = try_param(&lg_tuning::solve_streams, {1, 2, 3})) != LG_OK) return r;
   if ((r = try_param(&lg_tuning::chunk_mb, {256, 512, 1024, 2048, 4096})) != LG_OK) return r;
   if (mixed) {
     if (lg::gram_col_supported(g.ens)) {
-      if ((r = try_param(&lg_tuning::gram_kernel, {LG_GRAM_COLUMN, LG_GRAM_STREAM, LG_GRAM_QUEUE})) != LG_OK)
+      if ((r = try_param(&lg_tuning::gram_kernel, {LG_GRAM_COLUMN, LG_GRAM_COLUMN_LEAN,
+                                                   LG_GRAM_STREAM, LG_GRAM_QUEUE})) != LG_OK)
         return r;
     } else if ((r = try_param(&lg_tuning::gram_kernel, {LG_GRAM_STREAM, LG_GRAM_QUEUE})) != LG_OK) {
       return r;
@@ -1196,7 +1274,7 @@ int lg_autotune(lg_ctx* c, const double* xb, const double* axb, double* xa, doub
   }
   if ((r = try_param(&lg_tuning::ql_warps, {1, 2, 4})) != LG_OK) return r;
   if ((r = try_param(&lg_tuning::vec_warps, {2, 4, 8})) != LG_OK) return r;
-  if ((r = try_param(&lg_tuning::solve_streams, {1, 2})) != LG_OK) return r;
+
   cur.ms = best_ms;
   if ((r = lg_set_tuning(c, &cur)) != LG_OK) return r;
   // leave the context sized and captured for the chosen settings
@@ -1268,7 +1346,7 @@ void lg_destroy(lg_ctx* c) {
     if (e) cudaEventDestroy(e);
   for (auto& e : c->kev) cudaEventDestroy(e);
   dfree(c->d_work);
-  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  release_streams(c);
   delete c;
 }
 

@@ -457,55 +457,62 @@ void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, cons
                    const double* xb, const double* axb, double* xa, double* axa, double* tri,
                    double* lam, LT* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
                    int* overflow_list, int* overflow_n, int* eig_fail, int ql_warps,
-                   int vec_warps, cudaStream_t stream, cudaEvent_t ev_tri, cudaEvent_t ev_ql) {
+                   int vec_warps, int phases, cudaStream_t stream, cudaEvent_t ev_tri,
+                   cudaEvent_t ev_ql) {
   const int n = g.ens;
   constexpr size_t kSmemMax = 227 * 1024;
   const int ns = b.nsolves;
   if (ns == 0) return;
   // 1. tridiagonalisation
-  const size_t smem_t = sizeof(double) * ((size_t)n * (n + 1) / 2 + n);
-  cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t);
-  tridiag_kernel<<<ns, 32, smem_t, stream>>>(n, ns, C, tri);
-  if (ev_tri) record_event(ev_tri, stream);
-  // 2. QL, one solve per lane
-  ql_warps = std::max(1, std::min(ql_warps, (int)(kSmemMax / (sizeof(double) * 64 * n))));
-  const size_t smem_q = sizeof(double) * (size_t)ql_warps * 64 * n;
-  cudaFuncSetAttribute(ql_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_q);
-  const int ql_blocks = (ns + 32 * ql_warps - 1) / (32 * ql_warps);
-  ql_kernel<LT><<<ql_blocks, 32 * ql_warps, smem_q, stream>>>(
-      n, ns, (double)(n - 1) / g.inflation, tri, lam, rot_cs, rot_i, rot_n, rot_cap, overflow_list,
-      overflow_n, eig_fail);
-  if (ev_ql) record_event(ev_ql, stream);
-  // 3. vectors and update
-  const bool vertical = g.vert_dist > 0.0;
-  const int per = 1 + (vertical ? g.n_var : g.n);
-  const int slots = 32 / per;
-  const size_t vper = sizeof(VT) * ((size_t)32 * n + (size_t)slots * n);
-  const int vwarps = std::max(1, std::min(vec_warps, (int)(kSmemMax / vper)));
-  const size_t smem_v = sizeof(VT) * ((size_t)vwarps * 32 * n + (size_t)vwarps * slots * n);
-  cudaFuncSetAttribute(vec_kernel<VT, LT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem_v);
-  const int vblocks = (ns + slots * vwarps - 1) / (slots * vwarps);
-  vec_kernel<VT, LT><<<vblocks, 32 * vwarps, smem_v, stream>>>(g, b, t, tri, lam, rot_cs, rot_i,
-                                                               rot_n, rot_cap, xb, axb, xa, axa);
+  if (phases & kEigTridiag) {
+    const size_t smem_t = sizeof(double) * ((size_t)n * (n + 1) / 2 + n);
+    cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t);
+    tridiag_kernel<<<ns, 32, smem_t, stream>>>(n, ns, C, tri);
+    if (ev_tri) record_event(ev_tri, stream);
+  }
+  if (phases & kEigQL) {
+    // 2. QL, one solve per lane
+    ql_warps = std::max(1, std::min(ql_warps, (int)(kSmemMax / (sizeof(double) * 64 * n))));
+    const size_t smem_q = sizeof(double) * (size_t)ql_warps * 64 * n;
+    cudaFuncSetAttribute(ql_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_q);
+    const int ql_blocks = (ns + 32 * ql_warps - 1) / (32 * ql_warps);
+    ql_kernel<LT><<<ql_blocks, 32 * ql_warps, smem_q, stream>>>(
+        n, ns, (double)(n - 1) / g.inflation, tri, lam, rot_cs, rot_i, rot_n, rot_cap, overflow_list,
+        overflow_n, eig_fail);
+    if (ev_ql) record_event(ev_ql, stream);
+  }
+  if (phases & kEigVectors) {
+    // 3. vectors and update
+    const bool vertical = g.vert_dist > 0.0;
+    const int per = 1 + (vertical ? g.n_var : g.n);
+    const int slots = 32 / per;
+    const size_t vper = sizeof(VT) * ((size_t)32 * n + (size_t)slots * n);
+    const int vwarps = std::max(1, std::min(vec_warps, (int)(kSmemMax / vper)));
+    const size_t smem_v = sizeof(VT) * ((size_t)vwarps * 32 * n + (size_t)vwarps * slots * n);
+    cudaFuncSetAttribute(vec_kernel<VT, LT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem_v);
+    const int vblocks = (ns + slots * vwarps - 1) / (slots * vwarps);
+    vec_kernel<VT, LT><<<vblocks, 32 * vwarps, smem_v, stream>>>(g, b, t, tri, lam, rot_cs, rot_i,
+                                                                 rot_n, rot_cap, xb, axb, xa, axa);
+  }
 }
 
 void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
                  const double* xb, const double* axb, double* xa, double* axa, double* tri,
                  double* lam, void* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
                  int* overflow_list, int* overflow_n, int* eig_fail, bool fp32_vectors,
-                 int ql_warps, int vec_warps, cudaStream_t stream, cudaEvent_t ev_tri,
-                 cudaEvent_t ev_ql) {
+                 int ql_warps, int vec_warps, int phases, cudaStream_t stream,
+                 cudaEvent_t ev_tri, cudaEvent_t ev_ql) {
   if (fp32_vectors)
     launch_eig2_t<float, float2>(g, b, C, t, xb, axb, xa, axa, tri, lam,
                                  static_cast<float2*>(rot_cs), rot_i, rot_n, rot_cap,
-                                 overflow_list, overflow_n, eig_fail, ql_warps, vec_warps, stream,
-                                 ev_tri, ev_ql);
+                                 overflow_list, overflow_n, eig_fail, ql_warps, vec_warps, phases,
+                                 stream, ev_tri, ev_ql);
   else
     launch_eig2_t<double, double2>(g, b, C, t, xb, axb, xa, axa, tri, lam,
                                    static_cast<double2*>(rot_cs), rot_i, rot_n, rot_cap,
                                    overflow_list, overflow_n, eig_fail, ql_warps, vec_warps,
-                                   stream, ev_tri, ev_ql);
+                                   phases, stream, ev_tri, ev_ql);
 }
 
 }  // namespace lg

@@ -51,20 +51,22 @@ constexpr int kMmaWarp = kProducer + 1;         // warp 9
 constexpr int kThreads = kConv + 64;
 constexpr int kG = 8;                           // levels per work item
 constexpr int kN = 64;                          // accumulator columns per level
-constexpr int kRing = 6;                        // Y / record stages in flight
-constexpr int kOps = 4;                         // operand (A) buffers
 constexpr int kRows = 64;                       // records per stage (4 MMAs of K = 16)
 constexpr int kChunkA = 128 * 16 * 2;           // 4096 B: M = 128 x K = 16 BF16
 constexpr int kOpBytes = 4 * kChunkA;           // 16 KB
 constexpr int kYBytes = kRows * 64 * 4;         // 16 KB: 64 rows of 64 FP32
 constexpr int kDS = kN + 1;                     // accumulator copy row stride (odd)
-constexpr int kOffY = 0;
-constexpr int kOffOps = kOffY + kRing * kYBytes;
-constexpr int kOffRec = kOffOps + kOps * kOpBytes;
-constexpr int kOffW = kOffRec + kRing * kRows * 16;
-constexpr int kOffEnd = kOffW + 8 * 2 * kG * 16 * 4;  // per-warp sqrt(w), sqrt(w) d
-constexpr int kSmemBytes = kOffEnd;
-static_assert(128 * kDS * 4 <= kOps * kOpBytes, "accumulator copy must fit the operand buffers");
+// shared-memory layout for kRing Y/record stages and kOps operand buffers:
+// Y ring | operand buffers | record ring | sqrt(w), sqrt(w) d of the converter warps
+template <int kRing, int kOps>
+struct Layout {
+  static constexpr int kOffY = 0;
+  static constexpr int kOffOps = kOffY + kRing * kYBytes;
+  static constexpr int kOffRec = kOffOps + kOps * kOpBytes;
+  static constexpr int kOffW = kOffRec + kRing * kRows * 16;
+  static constexpr int kBytes = kOffW + 8 * 2 * kG * 16 * 4;
+  static_assert(128 * kDS * 4 <= kOps * kOpBytes, "accumulator copy must fit the operand buffers");
+};
 
 // instruction descriptor: kind::f16, BF16 A/B, FP32 D, K-major A and B, M = 128, N = 64
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
@@ -97,6 +99,30 @@ __device__ inline void cp_async_arrive(uint64_t* bar) {
 __device__ inline void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ inline void conv_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kConv) : "memory"); }
+
+// the two converter warps of quarter q (named barriers 2..5, 64 threads)
+__device__ inline void quarter_sync(int q) {
+  asm volatile("bar.sync %0, 64;" ::"r"(2 + q) : "memory");
+}
+
+// Gaspari-Cohn weight in FP32 for the mixed path (the polynomial of the
+// reference's schr2, letkf_yb.F90:262-286), with an approximate reciprocal:
+// its rounding is far below the BF16 split the weights feed.
+__device__ inline float gc_fast(float ri) {
+  if (ri > 2.0f) return 0.0f;
+  if (ri > 1.0f) {
+    float rj = ri * (1.0f / 12.0f) - 0.5f;
+    rj = rj * ri + 0.625f;
+    rj = rj * ri + 1.666667f;
+    return (rj * ri - 5.0f) * ri + 4.0f - __fdividef(0.6666667f, ri);
+  }
+  if (ri > 0.0f) {
+    const float rk = ri * ri;
+    const float rj = (-0.25f * ri + 0.5f) * ri + 0.625f;
+    return (rj * ri - 1.666667f) * rk + 1.0f;
+  }
+  return 1.0f;
+}
 
 // Wait for a phase, suspending between polls; gives up after 2 s of wall time
 // (raising the CTA's abort flag) or as soon as another thread has given up.
@@ -150,10 +176,18 @@ __device__ inline void item_levels(const SolveBatch& b, int item, int& col, int&
 
 }  // namespace colk
 
+// kRing: stages of records and ensemble rows in flight; kOps: operand buffers
+// between the converter warps and the MMA warp.  <6, 4> fills an SM's shared
+// memory (one CTA per SM, 178 KB); <3, 3> leaves ~120 KB of it to kernels of the
+// other solve streams (tridiagonalisation, QL) running beside it.
+template <int kRing, int kOps>
 __global__ void __launch_bounds__(colk::kThreads, 1)
     gram_col_kernel(Geometry g, HxDev hx, ListDev l, SolveBatch b, const double* axb,
                     double* Cout, double* tout, int* err, RecDev rec) {
   using namespace colk;
+  using Lay = Layout<kRing, kOps>;
+  constexpr int kOffY = Lay::kOffY, kOffOps = Lay::kOffOps, kOffRec = Lay::kOffRec,
+                kOffW = Lay::kOffW;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t full[kRing], empty[kRing], ready[kOps], opdone[kOps], tmem_free;
   __shared__ uint32_t tmem_base_sh;
@@ -318,10 +352,12 @@ __global__ void __launch_bounds__(colk::kThreads, 1)
     // ------------------------------------------------------------ converters
     const int m = tid & 63, q = tid >> 6;  // member; quarter q owns record groups q, q + 4
     const float inv_vd = vertical ? (float)(1.0 / g.vert_dist) : 0.0f;
-    float* SW = reinterpret_cast<float*>(smem + kOffW) + warp * (2 * kG * 16);  // [kG][16]
-    float* SD = SW + kG * 16;
+    // sqrt(w) and sqrt(w) d of a quarter's 16 records for the item's levels,
+    // [stage parity][quarter][sqrt(w) | sqrt(w) d][kG][16]: the two warps of a
+    // quarter compute alternate levels and meet on the quarter's named barrier
+    float* Wbase = reinterpret_cast<float*>(smem + kOffW);
     int cst = 0, p = 0;
-    unsigned long long nnz = 0;  // non-zero (record, level) weights, counted by warps 0, 2, 4, 6
+    unsigned long long nnz = 0;  // non-zero (record, level) weights, each counted once
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
       int col, kk0, G, w0, w1, u0, u1;
       float al;
@@ -332,36 +368,39 @@ __global__ void __launch_bounds__(colk::kThreads, 1)
 #pragma unroll
       for (int lv = 0; lv < kG; ++lv) tacc[lv] = 0.0f;
       bool ok = true;
-      for (int st = 0; st < nst && ok; ++st, ++cst) {
+      // Every converter warp runs all nst stages and reaches every quarter
+      // barrier, also after a failed wait (then it only skips the work), so the
+      // two warps of a quarter never wait for each other in vain.
+      for (int st = 0; st < nst; ++st, ++cst) {
         const int slot = cst % kRing;
-        if (!wait_warp(&full[slot], cst / kRing)) {
-          ok = false;
-          break;
-        }
+        if (ok) ok = wait_warp(&full[slot], cst / kRing);
         const int r0 = u0 + st * kRows;
         const float4* Rs = R + slot * kRows;
+        float* SW = Wbase + ((cst & 1) * 4 + q) * (2 * kG * 16);
+        float* SD = SW + kG * 16;
         {
-          // weights of this warp's 16 records (lane & 15) for every level (lane >> 4 + 2j)
+          // weights of the quarter's 16 records (lane & 15) for levels of this
+          // warp's parity: lv = (warp & 1) + 2 (lane >> 4) + 4 j
           const int r = lane & 15;
           const int row = r < 8 ? q * 8 + r : (q + 4) * 8 + (r - 8);
           const float4 rc = Rs[row];
 #pragma unroll
-          for (int j = 0; j < kG / 2; ++j) {
-            const int lv = (lane >> 4) + 2 * j;
+          for (int j = 0; j < kG / 4; ++j) {
+            const int lv = (warp & 1) + 2 * (lane >> 4) + 4 * j;
             const float lal = __shfl_sync(0xffffffffu, al, lv);
             const int lw0 = __shfl_sync(0xffffffffu, w0, lv), lw1 = __shfl_sync(0xffffffffu, w1, lv);
             float wt = rc.z, sw = 0.0f, sd = 0.0f;
             if (wt > 0.0f && r0 + row >= lw0 && r0 + row < lw1) {
               if (vertical) {
                 const float z = fabsf(lal - rc.y) * inv_vd;
-                wt *= g.gc_filter_vertical ? tc::schr2f(z) : (z > 2.0f ? 0.0f : 1.0f);
+                wt *= g.gc_filter_vertical ? gc_fast(z) : (z > 2.0f ? 0.0f : 1.0f);
               }
               if (wt > 0.0f) {
-                sw = sqrtf(wt);
+                sw = wt * rsqrtf(wt);
                 sd = rc.w * sw;
               }
             }
-            nnz += (sw > 0.0f && (warp & 1) == 0) ? 1u : 0u;
+            nnz += sw > 0.0f ? 1u : 0u;
             SW[lv * 16 + r] = sw;
             SD[lv * 16 + r] = sd;
           }
@@ -372,7 +411,8 @@ __global__ void __launch_bounds__(colk::kThreads, 1)
         for (int h = 0; h < 2; ++h)
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) y[h * 8 + jj] = Ys[((q + 4 * h) * 8 + jj) * 64 + m];
-        __syncwarp();
+        quarter_sync(q);  // both warps' weights of the quarter are written
+        if (!ok) continue;
         if (lane == 0) arrive(&empty[slot]);  // this warp has read the stage
 #pragma unroll
         for (int lv = 0; lv < kG; ++lv) {
@@ -480,7 +520,7 @@ bool gram_col_supported(int ens) { return ens <= 64 && ens % 4 == 0; }
 
 void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
                      const double* axb, double* C, double* t, int* err, const RecDev& rec,
-                     cudaStream_t stream) {
+                     bool lean, cudaStream_t stream) {
   if (b.nsolves == 0) return;
   static int sms = 0;
   if (sms == 0) {
@@ -492,10 +532,15 @@ void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const
   const int ngrp = (b.levels + colk::kG - 1) / colk::kG;
   const int nitems = b.ncols * ngrp;
   const int grid = std::min(nitems, sms);
-  cudaFuncSetAttribute(gram_col_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       colk::kSmemBytes);
-  gram_col_kernel<<<grid, colk::kThreads, colk::kSmemBytes, stream>>>(g, hx, l, b, axb, C, t,
-                                                                      err, rec);
+  if (lean) {
+    constexpr int bytes = colk::Layout<3, 3>::kBytes;
+    cudaFuncSetAttribute(gram_col_kernel<3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    gram_col_kernel<3, 3><<<grid, colk::kThreads, bytes, stream>>>(g, hx, l, b, axb, C, t, err, rec);
+  } else {
+    constexpr int bytes = colk::Layout<6, 4>::kBytes;
+    cudaFuncSetAttribute(gram_col_kernel<6, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    gram_col_kernel<6, 4><<<grid, colk::kThreads, bytes, stream>>>(g, hx, l, b, axb, C, t, err, rec);
+  }
 }
 
 }  // namespace lg

@@ -158,7 +158,7 @@ inline cudaError_t record_event(cudaEvent_t e, cudaStream_t st) {
 bool gram_col_supported(int ens);
 void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
                      const double* axb, double* C, double* t, int* err, const RecDev& rec,
-                     cudaStream_t stream);
+                     bool lean, cudaStream_t stream);
 void launch_gram_tc_stream(const Geometry& g, const HxDev& hx, const ListDev& l,
                            const SolveBatch& b, const double* axb, double* C, double* t, int* err,
                            const RecDev& rec, cudaStream_t stream);
@@ -169,11 +169,13 @@ void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, c
                       double* trans, double* wbar, int* eig_fail, cudaStream_t stream);
 size_t eig2_tri_doubles(int n);
 bool eig2_supported(const Geometry& g);
+// phases of launch_eig2 (a bit mask)
+constexpr int kEigTridiag = 1, kEigQL = 2, kEigVectors = 4, kEigAll = 7;
 void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
                  const double* xb, const double* axb, double* xa, double* axa, double* tri,
                  double* lam, void* rot_cs, unsigned char* rot_i, int* rot_n, int rot_cap,
                  int* overflow_list, int* overflow_n, int* eig_fail, bool fp32_vectors,
-                 int ql_warps, int vec_warps, cudaStream_t stream,
+                 int ql_warps, int vec_warps, int phases, cudaStream_t stream,
                  cudaEvent_t ev_after_tri = nullptr, cudaEvent_t ev_after_ql = nullptr);
 void launch_split_mean(int ens, int64_t npts_rows, const double* xb_in, double* xb, double* axb,
                        int* err, cudaStream_t stream);

@@ -81,7 +81,7 @@ class LgStats(C.Structure):
 
 
 # ----------------------------------------------------------------- configs
-LG_GRAM_AUTO, LG_GRAM_COLUMN, LG_GRAM_STREAM, LG_GRAM_QUEUE = 0, 1, 2, 3
+LG_GRAM_AUTO, LG_GRAM_COLUMN, LG_GRAM_STREAM, LG_GRAM_QUEUE, LG_GRAM_COLUMN_LEAN = 0, 1, 2, 3, 4
 
 
 class LgTuning(C.Structure):

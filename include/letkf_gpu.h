@@ -197,10 +197,13 @@ int lg_get_stats(const lg_ctx* ctx, lg_stats* st);
  * an FP64 result; in mixed precision the Gram variant and the ln p buckets only
  * change the FP32 summation order.  No reference counterpart: the reference
  * has no GPU path to tune. */
-#define LG_GRAM_AUTO 0   /* column groups where supported, else per-solve streaming */
+#define LG_GRAM_AUTO 0   /* column groups where supported (the lean variant with three
+                            solve streams), else per-solve streaming */
 #define LG_GRAM_COLUMN 1 /* one CTA per SM over (column, 8 levels) items, rows read once per group */
 #define LG_GRAM_STREAM 2 /* one CTA per solve streaming its ln p window of records */
 #define LG_GRAM_QUEUE 3  /* one CTA per solve compacting non-zero weights through a queue */
+#define LG_GRAM_COLUMN_LEAN 4 /* as LG_GRAM_COLUMN with a 3-stage ring (~110 KB of shared
+                                 memory), leaving room on each SM for other streams' kernels */
 
 typedef struct lg_tuning {
   int chunk_mb;    /* Gram workspace per solve chunk [MiB] (sets solves per launch), 16..65536 */
@@ -209,8 +212,9 @@ typedef struct lg_tuning {
                       the bucket boundaries that bound each level's record window */
   int ql_warps;    /* warps per block of the QL kernel, 1..6 */
   int vec_warps;   /* warps per block of the vector/update kernel, 1..8 */
-  int solve_streams; /* 1, or 2: chunks alternate between two streams with their own
-                        scratch, so one chunk's Gram overlaps another's eigensolve */
+  int solve_streams; /* 1; 2: chunks alternate between two streams with their own scratch;
+                        3: phase pipeline (Grams, eigensolves, vector updates on three
+                        streams, three buffer sets) */
   double ms;       /* device time of one analysis with these settings (lg_autotune) */
 } lg_tuning;
 
@@ -223,8 +227,8 @@ int lg_get_tuning(const lg_ctx* ctx, lg_tuning* out);
 int lg_set_tuning(lg_ctx* ctx, const lg_tuning* t);
 
 /* Autotuner: times complete analyses of the given device arrays (as
- * lg_run_device) over candidate settings -- chunk size, Gram variant, ln p
- * bucket count, QL and vector block shapes, solve streams -- one parameter at a time,
+ * lg_run_device) over candidate settings -- solve streams, chunk size, Gram
+ * variant, ln p bucket count, QL and vector block shapes -- one parameter at a time,
  * applies the fastest and returns it in *best (best->ms = its analysis time).
  * xa/axa are overwritten by the analyses. */
 int lg_autotune(lg_ctx* ctx, const double* d_xb, const double* d_axb, double* d_xa,

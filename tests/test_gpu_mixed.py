@@ -111,7 +111,7 @@ def test_tensor_core_gram_variants_agree(name, monkeypatch):
     axa_o = np.zeros_like(w.axb)
     o.analysis(w.xb, w.axb, xa_o, axa_o)
     got = {}
-    for kind in ("col", "stream", "queue"):
+    for kind in ("col", "lean", "stream", "queue"):
         monkeypatch.setenv("LETKF_GB300_GRAM", kind)
         ctx = lg.Letkf(cfg)
         ctx.set_obs(w.obs)
@@ -122,6 +122,6 @@ def test_tensor_core_gram_variants_agree(name, monkeypatch):
         errs = increment_rel_rms(cfg, w, (xa, axa), (xa_o, axa_o))
         assert max(errs.values()) <= TOL_INCREMENT, (kind, errs)
         got[kind] = (xa, axa)
-    for kind in ("stream", "queue"):
+    for kind in ("lean", "stream", "queue"):
         errs = increment_rel_rms(cfg, w, got[kind], got["col"])
         assert max(errs.values()) <= 1e-5, (kind, errs)

@@ -37,7 +37,7 @@ def test_set_tuning_validates_and_round_trips():
     t2 = ctx.tuning()
     assert (t2["chunk_mb"], t2["ql_warps"], t2["vec_warps"], t2["lnp_buckets"]) == (64, 2, 8, 32)
     for bad in ({"chunk_mb": 1}, {"ql_warps": 0}, {"ql_warps": 7}, {"vec_warps": 9},
-                {"lnp_buckets": 4}, {"gram_kernel": 9}, {"solve_streams": 3}):
+                {"lnp_buckets": 4}, {"gram_kernel": 9}, {"solve_streams": 4}):
         with pytest.raises(RuntimeError, match="LG_ERR_ARG"):
             ctx.set_tuning(**bad)
     ctx.letkf_final()
@@ -50,7 +50,8 @@ def test_fp64_analysis_is_bit_identical_under_every_setting():
     ctx.set_obs(w.obs)
     ref = None
     for kw in ({}, {"chunk_mb": 16}, {"ql_warps": 4, "vec_warps": 2}, {"vec_warps": 8},
-               {"solve_streams": 2, "chunk_mb": 16}):
+               {"solve_streams": 2, "chunk_mb": 16}, {"solve_streams": 3, "chunk_mb": 16},
+               {"solve_streams": 1}):
         ctx.set_tuning(**kw)
         xa = np.zeros_like(w.xb)
         axa = np.zeros_like(w.axb)
@@ -72,7 +73,8 @@ def test_autotune_mixed_keeps_the_increment_within_tolerance():
     xb, axb, xa, axa = _device_run(ctx, w)
     best = ctx.autotune(xb, axb, xa, axa)
     assert best["ms"] > 0.0
-    assert best["gram_kernel"] in (lg.LG_GRAM_COLUMN, lg.LG_GRAM_STREAM, lg.LG_GRAM_QUEUE)
+    assert best["gram_kernel"] in (lg.LG_GRAM_COLUMN, lg.LG_GRAM_COLUMN_LEAN, lg.LG_GRAM_STREAM,
+                                   lg.LG_GRAM_QUEUE)
     assert ctx.tuning()["chunk_mb"] == best["chunk_mb"]
     ctx.letkf_run_device(0, xb, axb, xa, axa)
     import torch

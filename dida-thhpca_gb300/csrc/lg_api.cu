@@ -85,7 +85,7 @@ struct lg_ctx {
   double lnp_span = 1.0;
   int boff_nb = 0;  // bucket count d_boff was sized for
   // launch shapes and bucket boundaries (lg_set_tuning / lg_autotune)
-  lg_tuning tune{1024, LG_GRAM_AUTO, 128, 1, 4, 3, 0.0};
+  lg_tuning tune{1024, LG_GRAM_AUTO, 128, 1, 4, 3, 0, 0.0};
   // status words: [0] err, [1] eig_fail
   int* d_status = nullptr;
   unsigned long long* d_band = nullptr;
@@ -95,7 +95,10 @@ struct lg_ctx {
   double *d_xin = nullptr, *d_spb = nullptr, *d_spa = nullptr;  // run_da_parallel staging
   size_t da_elems = 0;
   lg_stats stats{};
-  cudaEvent_t ev[5] = {};
+  // analysis timing: [0] start, [1] H(x) end, [2] solves start, [3] end,
+  // [4] selection start, [5] selection end
+  cudaEvent_t ev[6] = {};
+  cudaEvent_t ev_hx = nullptr;  // H(x) done (orders the records and Grams after it)
   std::vector<cudaEvent_t> kev;  // per-launch events of the solve phase
   unsigned long long* d_work = nullptr;
   // sizes fixed for the current observation set, and the captured analysis
@@ -376,6 +379,7 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
     return LG_ERR_CUDA;
   }
   for (auto& e : c->ev) cudaEventCreate(&e);
+  cudaEventCreateWithFlags(&c->ev_hx, cudaEventDisableTiming);
   Geometry& geo = c->geo;
   geo.ens = g.ens;
   geo.num_lat = g.num_lat;
@@ -843,10 +847,15 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   CK(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), st));
   CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
   CK(record_event(c->ev[0], st));
-  // H(x)
-  lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, st);
+  // H(x) on the side stream, beside the selection on st (the selection needs
+  // only observation positions; the records and Grams wait for H(x))
+  CK(cudaEventRecord(c->ev_fork, st));
+  CK(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
+  lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, c->side_stream);
   launches += c->obs.n_copies > 0;
-  CK(record_event(c->ev[1], st));
+  CK(record_event(c->ev[1], c->side_stream));
+  CK(cudaEventRecord(c->ev_hx, c->side_stream));
+  CK(record_event(c->ev[4], st));
   // selection: count, scan, fill (the lists' capacity was sized by prepare_capacity)
   const bool cells = c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH");
   if (cells)
@@ -860,6 +869,8 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   else
     lg::launch_search(geo, c->obs, c->lists, 1, nullptr, st);
   launches += 1;
+  CK(record_event(c->ev[5], st));
+  CK(cudaStreamWaitEvent(st, c->ev_hx, 0));
   const bool mixed_tc = g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k);
   lg::RecDev rec{};
   if (mixed_tc) {
@@ -933,7 +944,7 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     CK(record_event(kv[0], s_g));
     if (mixed_tc && (gram_kind == GramKind::kColumn || gram_kind == GramKind::kColumnLean))
       lg::launch_gram_col(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec,
-                          gram_kind == GramKind::kColumnLean, s_g);
+                          gram_kind == GramKind::kColumnLean, c->tune.gram_ctas, s_g);
     else if (mixed_tc && gram_kind == GramKind::kStream)
       lg::launch_gram_tc_stream(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec, s_g);
     else if (mixed_tc)
@@ -1068,7 +1079,7 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   }
   S.n_chunks = nchunks;
   S.ms_hx = elapsed_ms(c->ev[0], c->ev[1]);
-  S.ms_search = elapsed_ms(c->ev[1], c->ev[2]);
+  S.ms_search = elapsed_ms(c->ev[4], c->ev[5]);
   S.ms_solve = elapsed_ms(c->ev[2], c->ev[3]);
   S.ms_total = elapsed_ms(c->ev[0], c->ev[3]);
   S.n_launches = launches;
@@ -1204,7 +1215,7 @@ int lg_set_tuning(lg_ctx* c, const lg_tuning* t) {
   if (t->chunk_mb < 16 || t->chunk_mb > 65536 || t->gram_kernel < LG_GRAM_AUTO ||
       t->gram_kernel > LG_GRAM_COLUMN_LEAN || t->lnp_buckets < 8 || t->lnp_buckets > 1024 ||
       t->ql_warps < 1 || t->ql_warps > 6 || t->vec_warps < 1 || t->vec_warps > 8 ||
-      t->solve_streams < 1 || t->solve_streams > 3)
+      t->solve_streams < 1 || t->solve_streams > 3 || t->gram_ctas < 0 || t->gram_ctas > 4096)
     return LG_ERR_ARG;
   c->tune = *t;
   c->capacity_ready = false;  // chunk size and bucket count size buffers
@@ -1270,6 +1281,9 @@ int lg_autotune(lg_ctx* c, const double* xb, const double* axb, double* xa, doub
       return r;
     }
     if (vertical && (r = try_param(&lg_tuning::lnp_buckets, {32, 64, 128, 256, 512})) != LG_OK)
+      return r;
+    if ((cur.gram_kernel == LG_GRAM_COLUMN || cur.gram_kernel == LG_GRAM_COLUMN_LEAN) &&
+        (r = try_param(&lg_tuning::gram_ctas, {0, 76, 114})) != LG_OK)
       return r;
   }
   if ((r = try_param(&lg_tuning::ql_warps, {1, 2, 4})) != LG_OK) return r;
@@ -1344,6 +1358,7 @@ void lg_destroy(lg_ctx* c) {
   dfree(c->d_xin); dfree(c->d_spb); dfree(c->d_spa);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  if (c->ev_hx) cudaEventDestroy(c->ev_hx);
   for (auto& e : c->kev) cudaEventDestroy(e);
   dfree(c->d_work);
   release_streams(c);

@@ -520,7 +520,7 @@ bool gram_col_supported(int ens) { return ens <= 64 && ens % 4 == 0; }
 
 void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
                      const double* axb, double* C, double* t, int* err, const RecDev& rec,
-                     bool lean, cudaStream_t stream) {
+                     bool lean, int ctas, cudaStream_t stream) {
   if (b.nsolves == 0) return;
   static int sms = 0;
   if (sms == 0) {
@@ -531,7 +531,7 @@ void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const
   }
   const int ngrp = (b.levels + colk::kG - 1) / colk::kG;
   const int nitems = b.ncols * ngrp;
-  const int grid = std::min(nitems, sms);
+  const int grid = std::min(nitems, ctas > 0 ? ctas : sms);
   if (lean) {
     constexpr int bytes = colk::Layout<3, 3>::kBytes;
     cudaFuncSetAttribute(gram_col_kernel<3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);

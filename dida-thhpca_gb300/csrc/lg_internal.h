@@ -158,7 +158,7 @@ inline cudaError_t record_event(cudaEvent_t e, cudaStream_t st) {
 bool gram_col_supported(int ens);
 void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
                      const double* axb, double* C, double* t, int* err, const RecDev& rec,
-                     bool lean, cudaStream_t stream);
+                     bool lean, int ctas, cudaStream_t stream);
 void launch_gram_tc_stream(const Geometry& g, const HxDev& hx, const ListDev& l,
                            const SolveBatch& b, const double* axb, double* C, double* t, int* err,
                            const RecDev& rec, cudaStream_t stream);

@@ -88,7 +88,7 @@ class LgTuning(C.Structure):
     """lg_tuning: launch shapes and bucket boundaries (lg_set_tuning / lg_autotune)."""
     _fields_ = [("chunk_mb", C.c_int), ("gram_kernel", C.c_int), ("lnp_buckets", C.c_int),
                 ("ql_warps", C.c_int), ("vec_warps", C.c_int), ("solve_streams", C.c_int),
-                ("ms", C.c_double)]
+                ("gram_ctas", C.c_int), ("ms", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -215,6 +215,8 @@ typedef struct lg_tuning {
   int solve_streams; /* 1; 2: chunks alternate between two streams with their own scratch;
                         3: phase pipeline (Grams, eigensolves, vector updates on three
                         streams, three buffer sets) */
+  int gram_ctas;   /* persistent CTAs of the column Gram, 0 = one per SM; fewer leave
+                      whole SMs to the eigensolve beside it */
   double ms;       /* device time of one analysis with these settings (lg_autotune) */
 } lg_tuning;
 

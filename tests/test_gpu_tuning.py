@@ -37,7 +37,7 @@ def test_set_tuning_validates_and_round_trips():
     t2 = ctx.tuning()
     assert (t2["chunk_mb"], t2["ql_warps"], t2["vec_warps"], t2["lnp_buckets"]) == (64, 2, 8, 32)
     for bad in ({"chunk_mb": 1}, {"ql_warps": 0}, {"ql_warps": 7}, {"vec_warps": 9},
-                {"lnp_buckets": 4}, {"gram_kernel": 9}, {"solve_streams": 4}):
+                {"lnp_buckets": 4}, {"gram_kernel": 9}, {"solve_streams": 4}, {"gram_ctas": -1}):
         with pytest.raises(RuntimeError, match="LG_ERR_ARG"):
             ctx.set_tuning(**bad)
     ctx.letkf_final()

@@ -166,11 +166,14 @@ __device__ inline void level_window(const Geometry& g, const ListDev& l, const R
   w1 = bo[b_hi + 1];
 }
 
-// work item -> column and its first level (1-based) and level count
+// work item -> column and its first level (1-based) and level count.  Items are
+// numbered level-group-major, so that the round-robin assignment gives every
+// CTA a mix of level groups (near-surface groups have the longest record
+// windows; column-major numbering gave each CTA a single group whenever the
+// grid size was a multiple of the group count).
 __device__ inline void item_levels(const SolveBatch& b, int item, int& col, int& kk0, int& G) {
-  const int ngrp = (b.levels + kG - 1) / kG;
-  col = b.first_col + item / ngrp;
-  kk0 = (item % ngrp) * kG + 1;
+  col = b.first_col + item % b.ncols;
+  kk0 = (item / b.ncols) * kG + 1;
   G = min(kG, b.levels - kk0 + 1);
 }
 

@@ -331,7 +331,8 @@ def main():
     achieved = dom.get("achieved_tflops", 0.0)
     launches_dom = max(1, iso["n_chunks"])
     traffic = None
-    if dom_name in PROFILED_DRAM_BYTES_PER_SOLVE:
+    # the profiled figures are of the mixed path's kernels (column Gram, tridiag)
+    if dom_name in PROFILED_DRAM_BYTES_PER_SOLVE and (mixed or dom_name != "gram"):
         traffic = PROFILED_DRAM_BYTES_PER_SOLVE[dom_name] * solves / launches_dom
     roofline = {"bound": dom["bound"], "kernel": dom_name, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": traffic,
@@ -345,7 +346,9 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": "bf16/f32 contractions, f64 eig" if cfg.precision == lg.LG_PREC_MIXED else "f64",
-        "data": "synthetic (seeded spherical-harmonic ensemble, uniform observations)",
+        "data": "synthetic (seeded spherical-harmonic ensemble, %s observations)" % (
+            "uniform" if not cfg.clustered_frac else
+            f"{int(100 * cfg.clustered_frac)}% clustered + uniform"),
         "config": {"workload": f"{cfg.name}: {cfg.num_lon}x{cfg.num_lat}x{cfg.nz}, ps/u/v/pt, "
                                f"N={cfg.ens}, {cfg.n_obs} obs, L={cfg.local_dist:g} km, "
                                f"vert {cfg.vert_dist:g} ln p, rho={cfg.inflation}",

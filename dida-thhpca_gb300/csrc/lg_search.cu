@@ -254,6 +254,41 @@ __device__ inline bool keep_copy(const Geometry& g, const ObsDev& ob, int j, flo
   return keep;
 }
 
+// position of the n-th (0-based) set bit of w, by halving the window
+__device__ inline int nth_set_bit(unsigned w, int n) {
+  int pos = 0;
+#pragma unroll
+  for (int sh = 16; sh > 0; sh >>= 1) {
+    const unsigned low = w & ((1u << sh) - 1u);
+    const int c = __popc(low);
+    if (n >= c) {
+      n -= c;
+      w >>= sh;
+      pos += sh;
+    } else {
+      w = low;
+    }
+  }
+  return pos;
+}
+
+// Gaspari-Cohn in FP32 for the mixed path's weights (the polynomial of schr2)
+__device__ inline float schr2_f32(float ri) {
+  if (ri > 2.0f) return 0.0f;
+  if (ri > 1.0f) {
+    float rj = ri * (1.0f / 12.0f) - 0.5f;
+    rj = rj * ri + 0.625f;
+    rj = rj * ri + 1.666667f;
+    return (rj * ri - 5.0f) * ri + 4.0f - 0.6666667f / ri;
+  }
+  if (ri > 0.0f) {
+    const float rk = ri * ri;
+    const float rj = (-0.25f * ri + 0.5f) * ri + 0.625f;
+    return (rj * ri - 1.666667f) * rk + 1.0f;
+  }
+  return 1.0f;
+}
+
 __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob, CellIndex ci,
                                                            ListDev l, int fill, SearchArgs sa,
                                                            unsigned long long* band) {
@@ -352,37 +387,50 @@ __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob
         continue;
       }
       __syncwarp();
-      // emit the kept copies of this segment in position (observation-index) order
+      // Emit the kept copies of this segment in position (observation-index)
+      // order, 32 bitmap words at a time.  The kept copies of the block are
+      // dealt one per lane (copy t of the block to lane t mod 32) rather than
+      // word by word, so that every lane evaluates a weight: the weights are
+      // FP64 work and the words hold very different numbers of kept copies.
       const int words = (len + 31) / 32;
       for (int wb = 0; wb < words && !done; wb += 32) {
         const int wd = wb + (int)lane;
         const unsigned int bits = wd < words ? bitmap[wd] : 0u;
-        const int cnt = __popc(bits) * nent;
-        int incl = cnt;
+        int incl = __popc(bits);  // kept copies up to and including this lane's word
 #pragma unroll
         for (int sft = 1; sft < 32; sft <<= 1) {
           const int v = __shfl_up_sync(0xffffffffu, incl, sft);
           if ((int)lane >= sft) incl += v;
         }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        int64_t posw = written + incl - cnt;
-        unsigned int rem = bits;
-        while (rem) {
-          const int bit = __ffs(rem) - 1;
-          rem &= rem - 1;
-          const int j = j0 + wd * 32 + bit;
+        const int kept = __shfl_sync(0xffffffffu, incl, 31);
+        for (int t0 = 0; t0 < kept; t0 += 32) {
+          const int t = t0 + (int)lane;
+          // word holding kept copy t: the first lane whose inclusive count exceeds t
+          int wl = 0;
+#pragma unroll
+          for (int step = 16; step > 0; step >>= 1) {
+            const int v = __shfl_sync(0xffffffffu, incl, wl + step - 1);
+            if (v <= t) wl += step;
+          }
+          const unsigned int wbits = __shfl_sync(0xffffffffu, bits, wl & 31);
+          const int before = __shfl_sync(0xffffffffu, incl, wl & 31) - __popc(wbits);
+          if (t >= kept) continue;
+          const int bit = nth_set_bit(wbits, t - before);
+          const int j = j0 + (wb + wl) * 32 + bit;
           const int o = ob.copy_obs[j];
-          double ri;
+          double gc;
           if (exact_rloc) {
             const double dist = latlon_dist_pre(ob.dcx[o], ob.dsx[o], ob.dyr[o], ccx, csx, cyr);
-            ri = __ddiv_rn(__dmul_rn(dist, 1.0), g.local_dist);
+            const double ri = __ddiv_rn(__dmul_rn(dist, 1.0), g.local_dist);
+            // a copy kept by the exact test has ri <= 2; clamp rounding beyond it
+            gc = loc_fn(fmin(ri, 2.0), g.gc_filter);
           } else {  // mixed path: the weight only needs FP32 accuracy
             const float v32 = fminf(ob.fcx[o] * fcx * cosf(ob.fyr[o] - fyr) + ob.fsx[o] * fsx, 1.0f);
-            ri = (double)(6371.393f * acosf(v32) / (float)g.local_dist);
+            const float ri = fminf(6371.393f * acosf(v32) / (float)g.local_dist, 2.0f);
+            gc = (double)(g.gc_filter ? schr2_f32(ri) : 1.0f);
           }
-          // a copy kept by the exact test has ri <= 2; clamp rounding beyond it
-          const double gc = loc_fn(fmin(ri, 2.0), g.gc_filter);
           const int e0 = ob.copy_eoff[j];
+          int64_t posw = written + (int64_t)t * nent;
           for (int m = 0; m < nent; ++m, ++posw) {
             if (posw < cap) {
               l.ent[out0 + posw] = e0 + m;
@@ -390,7 +438,7 @@ __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob
             }
           }
         }
-        written += total;
+        written += (int64_t)kept * nent;
         if (written >= cap) done = true;
       }
       __syncwarp();

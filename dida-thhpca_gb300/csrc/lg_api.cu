@@ -919,7 +919,6 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   // start, [1] Gram end, [2] eigensolve start, [3] after tridiag, [4] after QL,
   // [5] vectors start, [6] vectors end.
   const int nl = c->tune.solve_streams;
-  const bool vec_on_eig = getenv("LETKF_GB300_VEC_ON_EIG") != nullptr;
   if (nl >= 2) {
     CK(cudaEventRecord(c->ev_fork, st));
     CK(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
@@ -931,7 +930,7 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     lg_ctx::SolveLane& L = c->lane[set];
     cudaStream_t s = (nl == 2 && (q & 1)) ? c->side_stream : st;
     cudaStream_t s_g = nl == 3 ? c->side_stream : s, s_e = s;
-    cudaStream_t s_v = (nl == 3 && !vec_on_eig) ? c->third_stream : s;
+    cudaStream_t s_v = nl == 3 ? c->third_stream : s;
     cudaEvent_t* kv = &c->kev[7 * q];
     lg::SolveBatch b{};
     b.mode = 0;

@@ -696,6 +696,18 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
     rr |= upload(c, cell_off.data(), cell_off.size(), &d_cell_off);
     rr |= upload(c, cell_start.data(), cell_start.size(), &d_cell_start);
     rr |= upload(c, perm.data(), perm.size(), &d_perm);
+    // per slot: its observation, then the candidate data gathered on the device
+    std::vector<int> slot_obs(ncopies);
+    for (int sg = 0; sg < nseg; ++sg)
+      for (int j = bt_off[sg]; j < bt_off[sg + 1]; ++j)
+        slot_obs[j] = c->h_copy_obs[bt_off[sg] + perm[j]];
+    const int* d_slot_obs = nullptr;
+    float4* d_cand = nullptr;
+    rr |= upload(c, slot_obs.data(), slot_obs.size(), &d_slot_obs);
+    rr |= scratch(c, (size_t)ncopies, &d_cand);
+    if (rr == LG_OK)
+      lg::launch_cell_cands(c->obs, g.obs_polar, d_slot_obs, (int)ncopies, d_cand, c->own_stream);
+    ci.cand = d_cand;
     if (rr != LG_OK) {
       free_obs(c);
       return LG_ERR_NOMEM;

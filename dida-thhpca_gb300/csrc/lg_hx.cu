@@ -34,6 +34,25 @@ __global__ void obs_trig_kernel(int n, const double* lat, const double* lon, dou
   fyr[o] = (float)lon[o] / 180.0f * pf;
 }
 
+// the selection's per-slot candidate data, gathered once per observation set so
+// that the candidate loop reads one contiguous float4 instead of chasing
+// copy -> observation -> trigonometry
+__global__ void cell_cands_kernel(ObsDev o, double obs_polar, const int* slot_obs, int nslots,
+                                  float4* cand) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslots) return;
+  const int ob = slot_obs[s];
+  cand[s] = make_float4(o.fcx[ob], o.fsx[ob], o.fyr[ob],
+                        fabs(o.olat[ob]) <= obs_polar ? 1.0f : 0.0f);
+}
+
+void launch_cell_cands(const ObsDev& o, double obs_polar, const int* slot_obs, int nslots,
+                       float4* cand, cudaStream_t stream) {
+  if (nslots == 0) return;
+  cell_cands_kernel<<<(nslots + 255) / 256, 256, 0, stream>>>(o, obs_polar, slot_obs, nslots,
+                                                              cand);
+}
+
 void launch_obs_trig(const ObsDev& o, double* dcx, double* dsx, double* dyr, float* fcx,
                      float* fsx, float* fyr, cudaStream_t stream) {
   if (o.n_obs == 0) return;

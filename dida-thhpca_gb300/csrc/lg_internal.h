@@ -76,6 +76,8 @@ struct CellIndex {
   const int* cell_off;     // per segment: offset of its cell_start block
   const int* cell_start;   // per segment: nrows*ncols+1 offsets into perm
   const int* perm;         // per copy slot: segment positions sorted by cell
+  const float4* cand;      // per copy slot, in perm order: the observation's FP32 cos(lat),
+                           // sin(lat), lon [rad] and 1 if |lat| <= obs_polar, else 0
 };
 
 // H(x) results per copy entry.
@@ -125,6 +127,9 @@ struct SolveBatch {
 };
 
 // kernels (host launchers), all asynchronous on `stream`
+// cand[slot] of every copy slot (slot_obs[slot] = observation of the slot)
+void launch_cell_cands(const ObsDev& o, double obs_polar, const int* slot_obs, int nslots,
+                       float4* cand, cudaStream_t stream);
 void launch_obs_trig(const ObsDev& o, double* dcx, double* dsx, double* dyr, float* fcx,
                      float* fsx, float* fyr, cudaStream_t stream);
 void set_type_table(const TypeTable& t, cudaStream_t stream);

@@ -352,6 +352,7 @@ __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob
       const int4 box = ci.box[seg];                                // row0, nrows, col0, ncols
       const int* cs = ci.cell_start + ci.cell_off[seg];
       const int* perm = ci.perm + j0;
+      const float4* cand = ci.cand + j0;
       if (fill)
         for (int wd = lane; wd < (len + 31) / 32; wd += 32) bitmap[wd] = 0u;
       __syncwarp();
@@ -370,8 +371,16 @@ __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob
             int pos = 0;
             if (i < i1) {
               pos = perm[i];
-              keep = keep_copy(g, ob, j0 + pos, fcx, fsx, fyr, ccx, csx, cyr, sa, false, nullptr,
-                               fill ? nullptr : &nband);
+              const float4 cd = cand[i];
+              if (cd.w != 0.0f) {  // within obs_polar
+                const float v32 = cd.x * fcx * cosf(cd.z - fyr) + cd.y * fsx;
+                if (v32 > sa.vhi) {
+                  keep = true;
+                } else if (v32 >= sa.vlo) {  // in the band: the exact FP64 test
+                  keep = keep_copy(g, ob, j0 + pos, fcx, fsx, fyr, ccx, csx, cyr, sa, false,
+                                   nullptr, fill ? nullptr : &nband);
+                }
+              }
             }
             if (fill) {
               if (keep) atomicOr(&bitmap[pos >> 5], 1u << (pos & 31));

@@ -55,8 +55,11 @@ __device__ inline size_t uoff(int i) { return (size_t)i * (i - 1) / 2; }   // ro
 // is two fused multiply-adds per element.
 __device__ inline int tri_idx(int j) { return j * (j + 1) / 2; }
 
+// u32 = 1 (mixed path): the reflectors are written in FP32 for the FP32 vector
+// kernel -- U as floats at the start of the U region and 1/h as floats after
+// them -- so that kernel converts nothing; the double H is kept for reference.
 __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const double* Cin,
-                                                     double* tri) {
+                                                     double* tri, int u32) {
   const int s = blockIdx.x;
   if (s >= nsolves) return;
   const int lane = threadIdx.x;
@@ -93,10 +96,12 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
     return v;
   };
   constexpr double kTiny = 0x1p-900, kHuge = 0x1p900;
+  float* U32 = reinterpret_cast<float*>(U);
+  float* Hinv32 = U32 + (size_t)n * (n - 1) / 2;
   for (int i = n - 1; i >= 1; --i) {
     const int l = i - 1;
     double* row = P + tri_idx(i);  // u: row i, columns 0..l
-    double h = 0.0, ei;
+    double h = 0.0, ei, hinv = 0.0;
     if (l > 0) {
       double ss = 0.0;
       for (int c = lane; c <= l; c += 32) ss = fma(row[c], row[c], ss);
@@ -130,6 +135,7 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
         // p = A u / h, lane j over row j: columns c <= j from row j, c > j from
         // column j (the same trip count on every lane)
         const double inv_h = 1.0 / h;
+        hinv = inv_h;
         double fs = 0.0;
         for (int j = lane; j <= l; j += 32) {
           const int tj = tri_idx(j);
@@ -170,7 +176,12 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
       ei = row[l];
     }
     // reflector of step i: u = row i (scaled), h
-    for (int c = lane; c < i; c += 32) U[e2::uoff(i) + c] = row[c];
+    if (u32) {
+      for (int c = lane; c < i; c += 32) U32[e2::uoff(i) + c] = (float)row[c];
+      if (lane == 0) Hinv32[i] = (float)hinv;
+    } else {
+      for (int c = lane; c < i; c += 32) U[e2::uoff(i) + c] = row[c];
+    }
     if (lane == 0) {
       H[i] = h;
       E[i] = ei;
@@ -181,6 +192,7 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
   if (lane == 0) {
     H[0] = 0.0;
     E[0] = 0.0;
+    if (u32) Hinv32[0] = 0.0f;
   }
 }
 
@@ -196,7 +208,7 @@ __device__ inline float2 make_rot<float2>(double c, double s) { return make_floa
 // LT: element type of the rotation log (double2 for the FP64 path, float2 when the
 // rotations are only replayed in FP32 by the mixed-precision vector kernel)
 template <typename LT>
-__global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shift,
+__global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shift, double srho,
                                                  const double* tri, double* lam, LT* rot_cs,
                                                  unsigned char* rot_i, int* rot_n, int rot_cap,
                                                  int* overflow_list, int* overflow_n,
@@ -296,7 +308,18 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
     }
   }
   if (!live) return;
-  for (int i = 0; i < n; ++i) lam[(size_t)s * n + i] = DD(i) * 1.0 + shift;
+  if constexpr (sizeof(LT) == sizeof(float2)) {
+    // mixed path: the FP32 vector kernel's per-eigenvalue factors, computed once
+    // here in FP64: 1/lambda_j and sqrt((k-1)/lambda_j) - sqrt(rho)
+    float2* fl = reinterpret_cast<float2*>(lam + (size_t)s * n);
+    const double km1 = (double)(n - 1);
+    for (int i = 0; i < n; ++i) {
+      const double li = DD(i) * 1.0 + shift;
+      fl[i] = make_float2((float)(1.0 / li), (float)(sqrt(km1 / li) - srho));
+    }
+  } else {
+    for (int i = 0; i < n; ++i) lam[(size_t)s * n + i] = DD(i) * 1.0 + shift;
+  }
   rot_n[s] = over ? -1 : nrot;
   if (fail) atomicAdd(eig_fail, 1);
   if (over) overflow_list[atomicAdd(overflow_n, 1)] = s;
@@ -315,6 +338,7 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
                                                   const unsigned char* rot_i, const int* rot_n,
                                                   int rot_cap, const double* xb,
                                                   const double* axb, double* xa, double* axa) {
+  constexpr bool kF32 = sizeof(VT) == sizeof(float);  // mixed path: FP32 reflectors and factors
   const int n = g.ens;
   const bool vertical = g.vert_dist > 0.0;
   const int nvec_max = 1 + (vertical ? g.n_var : g.n);
@@ -366,17 +390,31 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
       const double* xr = xb + (size_t)n * (r_state + (size_t)g.n * ci);
       for (int i = 0; i < n; ++i) YY(i) = (VT)xr[i];
     }
-    const double* H = T + 2 * n;
-    const double* U = T + 3 * n;
     // y = Q^T x = P_1 ... P_{n-1} x  (P_{n-1} first)
-    for (int i = n - 1; i >= 1; --i) {
-      const double h = H[i];
-      if (h == 0.0) continue;
-      const double* u = U + e2::uoff(i);
-      VT dot = 0;
-      for (int kk = 0; kk < i; ++kk) dot += (VT)u[kk] * YY(kk);
-      dot /= (VT)h;
-      for (int kk = 0; kk < i; ++kk) YY(kk) -= (VT)u[kk] * dot;
+    if constexpr (kF32) {
+      const float* U32 = reinterpret_cast<const float*>(T + 3 * n);
+      const float* Hinv32 = U32 + (size_t)n * (n - 1) / 2;
+      for (int i = n - 1; i >= 1; --i) {
+        const float hinv = Hinv32[i];
+        if (hinv == 0.0f) continue;
+        const float* u = U32 + e2::uoff(i);
+        float dot = 0.0f;
+        for (int kk = 0; kk < i; ++kk) dot += u[kk] * YY(kk);
+        dot *= hinv;
+        for (int kk = 0; kk < i; ++kk) YY(kk) -= u[kk] * dot;
+      }
+    } else {
+      const double* H = T + 2 * n;
+      const double* U = T + 3 * n;
+      for (int i = n - 1; i >= 1; --i) {
+        const double h = H[i];
+        if (h == 0.0) continue;
+        const double* u = U + e2::uoff(i);
+        VT dot = 0;
+        for (int kk = 0; kk < i; ++kk) dot += (VT)u[kk] * YY(kk);
+        dot /= (VT)h;
+        for (int kk = 0; kk < i; ++kk) YY(kk) -= (VT)u[kk] * dot;
+      }
     }
     // y = Z^T y: rotations in generation order
     const LT* cs = rot_cs + (size_t)s * rot_cap;
@@ -390,7 +428,12 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
     }
     if (v == 0) {
       VT* ts = tslot + (size_t)q * n;
-      for (int j = 0; j < n; ++j) ts[j] = (VT)((double)YY(j) / L[j]);
+      if constexpr (kF32) {
+        const float2* fl = reinterpret_cast<const float2*>(L);
+        for (int j = 0; j < n; ++j) ts[j] = YY(j) * fl[j].x;
+      } else {
+        for (int j = 0; j < n; ++j) ts[j] = (VT)((double)YY(j) / L[j]);
+      }
     }
   }
   __syncwarp();
@@ -401,10 +444,18 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
   const double srho = sqrt(g.inflation);
   if (work && v >= 1) {
     const VT* ts = tslot + (size_t)q * n;
-    const double km1 = (double)(n - 1);
-    for (int j = 0; j < n; ++j) {
-      dotw += YY(j) * ts[j];
-      YY(j) *= (VT)(sqrt(km1 / L[j]) - srho);
+    if constexpr (kF32) {
+      const float2* fl = reinterpret_cast<const float2*>(L);
+      for (int j = 0; j < n; ++j) {
+        dotw += YY(j) * ts[j];
+        YY(j) *= fl[j].y;
+      }
+    } else {
+      const double km1 = (double)(n - 1);
+      for (int j = 0; j < n; ++j) {
+        dotw += YY(j) * ts[j];
+        YY(j) *= (VT)(sqrt(km1 / L[j]) - srho);
+      }
     }
     // y = Z y: rotations in reverse order
     const LT* cs = rot_cs + (size_t)s * rot_cap;
@@ -417,16 +468,30 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
       YY(i + 1) = -(VT)c.y * a0 + (VT)c.x * a1;
     }
     // y = Q y = P_{n-1} ... P_1 y  (P_1 first)
-    const double* H = T + 2 * n;
-    const double* U = T + 3 * n;
-    for (int i = 1; i < n; ++i) {
-      const double h = H[i];
-      if (h == 0.0) continue;
-      const double* u = U + e2::uoff(i);
-      VT dot = 0;
-      for (int kk = 0; kk < i; ++kk) dot += (VT)u[kk] * YY(kk);
-      dot /= (VT)h;
-      for (int kk = 0; kk < i; ++kk) YY(kk) -= (VT)u[kk] * dot;
+    if constexpr (kF32) {
+      const float* U32 = reinterpret_cast<const float*>(T + 3 * n);
+      const float* Hinv32 = U32 + (size_t)n * (n - 1) / 2;
+      for (int i = 1; i < n; ++i) {
+        const float hinv = Hinv32[i];
+        if (hinv == 0.0f) continue;
+        const float* u = U32 + e2::uoff(i);
+        float dot = 0.0f;
+        for (int kk = 0; kk < i; ++kk) dot += u[kk] * YY(kk);
+        dot *= hinv;
+        for (int kk = 0; kk < i; ++kk) YY(kk) -= u[kk] * dot;
+      }
+    } else {
+      const double* H = T + 2 * n;
+      const double* U = T + 3 * n;
+      for (int i = 1; i < n; ++i) {
+        const double h = H[i];
+        if (h == 0.0) continue;
+        const double* u = U + e2::uoff(i);
+        VT dot = 0;
+        for (int kk = 0; kk < i; ++kk) dot += (VT)u[kk] * YY(kk);
+        dot /= (VT)h;
+        for (int kk = 0; kk < i; ++kk) YY(kk) -= (VT)u[kk] * dot;
+      }
     }
     // xa = axb + sqrt(rho) x + (W - sqrt(rho) I) x + overline_w . x, recentred
     const double ab = axb[r_state + (size_t)g.n * ci];
@@ -467,7 +532,7 @@ void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, cons
   if (phases & kEigTridiag) {
     const size_t smem_t = sizeof(double) * ((size_t)n * (n + 1) / 2 + n);
     cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t);
-    tridiag_kernel<<<ns, 32, smem_t, stream>>>(n, ns, C, tri);
+    tridiag_kernel<<<ns, 32, smem_t, stream>>>(n, ns, C, tri, sizeof(VT) == sizeof(float) ? 1 : 0);
     if (ev_tri) record_event(ev_tri, stream);
   }
   if (phases & kEigQL) {
@@ -477,8 +542,8 @@ void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, cons
     cudaFuncSetAttribute(ql_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_q);
     const int ql_blocks = (ns + 32 * ql_warps - 1) / (32 * ql_warps);
     ql_kernel<LT><<<ql_blocks, 32 * ql_warps, smem_q, stream>>>(
-        n, ns, (double)(n - 1) / g.inflation, tri, lam, rot_cs, rot_i, rot_n, rot_cap, overflow_list,
-        overflow_n, eig_fail);
+        n, ns, (double)(n - 1) / g.inflation, sqrt(g.inflation), tri, lam, rot_cs, rot_i, rot_n,
+        rot_cap, overflow_list, overflow_n, eig_fail);
     if (ev_ql) record_event(ev_ql, stream);
   }
   if (phases & kEigVectors) {

@@ -55,6 +55,21 @@ __device__ inline size_t uoff(int i) { return (size_t)i * (i - 1) / 2; }   // ro
 // is two fused multiply-adds per element.
 __device__ inline int tri_idx(int j) { return j * (j + 1) / 2; }
 
+// 1/x by the Newton-Raphson iteration r <- r + r (1 - x r) from the hardware
+// approximation (PTX rcp.approx.ftz.f64); two steps reach full double
+// precision for the reflector norms here (normal numbers, checked before).
+__device__ inline double rcp_nr(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+
+// biased exponent of a double (0 for zero and subnormals, 2047 for inf/NaN)
+__device__ inline int dexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
+
 // u32 = 1 (mixed path): the reflectors are written in FP32 for the FP32 vector
 // kernel -- U as floats at the start of the U region and 1/h as floats after
 // them -- so that kernel converts nothing; the double H is kept for reference.
@@ -95,7 +110,6 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
   };
-  constexpr double kTiny = 0x1p-900, kHuge = 0x1p900;
   float* U32 = reinterpret_cast<float*>(U);
   float* Hinv32 = U32 + (size_t)n * (n - 1) / 2;
   for (int i = n - 1; i >= 1; --i) {
@@ -107,7 +121,9 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
       for (int c = lane; c <= l; c += 32) ss = fma(row[c], row[c], ss);
       double h0 = wsum(ss);
       double sc = 1.0;
-      if (!(h0 >= kTiny && h0 <= kHuge) && h0 != 0.0) {
+      // outside [2^-900, 2^900] (checked on the exponent bits), and not zero
+      const int eh = dexp(h0);
+      if ((eh < 1023 - 900 || eh > 1023 + 900) && h0 != 0.0) {
         // extreme magnitudes: scale the row by its 1-norm first (as tred2 does)
         double a1 = 0.0;
         for (int c = lane; c <= l; c += 32) a1 += fabs(row[c]);
@@ -134,7 +150,7 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
         __syncwarp();
         // p = A u / h, lane j over row j: columns c <= j from row j, c > j from
         // column j (the same trip count on every lane)
-        const double inv_h = 1.0 / h;
+        const double inv_h = rcp_nr(h);
         hinv = inv_h;
         double fs = 0.0;
         for (int j = lane; j <= l; j += 32) {

@@ -1315,6 +1315,17 @@ int lg_get_stats(const lg_ctx* c, lg_stats* st) {
   return LG_OK;
 }
 
+int lg_get_timeline(const lg_ctx* c, float* ms, int cap, int* nchunks) {
+  if (!c || !nchunks || cap < 0) return LG_ERR_ARG;
+  const int nq = (int)c->stats.n_chunks;
+  *nchunks = nq;
+  if (!ms) return LG_OK;
+  if (nq <= 0 || (int)c->kev.size() < 7 * nq) return LG_ERR_STATE;
+  const int n = std::min(cap, 7 * nq);
+  for (int i = 0; i < n; ++i) ms[i] = elapsed_ms(c->ev[0], c->kev[i]);
+  return LG_OK;
+}
+
 int lg_get_lists(const lg_ctx* c, int* counts, int* entries, double* rloc, int64_t* total) {
   if (!c || !total) return LG_ERR_ARG;
   if (!c->lists.off) return LG_ERR_STATE;

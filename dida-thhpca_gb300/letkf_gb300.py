@@ -287,6 +287,7 @@ def load_library(path: str = LIB_PATH):
     lib.lg_run_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p]
     lib.lg_get_stats.argtypes = [C.c_void_p, P(LgStats)]
+    lib.lg_get_timeline.argtypes = [C.c_void_p, P(C.c_float), C.c_int, P(C.c_int)]
     lib.lg_get_tuning.argtypes = [C.c_void_p, P(LgTuning)]
     lib.lg_set_tuning.argtypes = [C.c_void_p, P(LgTuning)]
     lib.lg_autotune.argtypes = [C.c_void_p] + [C.c_void_p] * 5 + [P(LgTuning)]
@@ -434,6 +435,17 @@ class Letkf:
         st = LgStats()
         check(self.lib.lg_get_stats(self.h, C.byref(st)), "lg_get_stats")
         return st.as_dict()
+
+    def timeline(self) -> np.ndarray:
+        """lg_get_timeline: [chunks, 7] ms after the analysis start (Gram
+        start/end, eigensolve start, tridiag end, QL end, vectors start/end)."""
+        nq = C.c_int()
+        check(self.lib.lg_get_timeline(self.h, None, 0, C.byref(nq)), "lg_get_timeline")
+        ms = np.zeros(max(1, 7 * nq.value), np.float32)
+        if nq.value:
+            check(self.lib.lg_get_timeline(self.h, _ptr(ms, C.c_float), 7 * nq.value,
+                                           C.byref(nq)), "lg_get_timeline")
+        return ms[:7 * nq.value].reshape(nq.value, 7)
 
     def lists(self):
         total = C.c_int64()

@@ -193,6 +193,14 @@ int lg_run_da_parallel(lg_ctx* ctx, int ntimes, double gamma1, double gamma2, do
 /* Statistics of the last lg_run. */
 int lg_get_stats(const lg_ctx* ctx, lg_stats* st);
 
+/* Timeline of the last lg_run's solve phase: for each chunk of columns, seven
+ * instants in ms after the analysis started -- Gram start, Gram end,
+ * eigensolve start, tridiagonalisation end, QL end, vector update start,
+ * vector update end -- at ms[7*q .. 7*q+6].  Writes min(cap, 7*chunks) values;
+ * *nchunks receives the chunk count (ms may be NULL to query it).  Diagnostic
+ * only; no reference counterpart. */
+int lg_get_timeline(const lg_ctx* ctx, float* ms, int cap, int* nchunks);
+
 /* Launch shapes and bucket boundaries of the analysis.  None of them changes
  * an FP64 result; in mixed precision the Gram variant and the ln p buckets only
  * change the FP32 summation order.  No reference counterpart: the reference

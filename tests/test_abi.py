@@ -46,6 +46,7 @@ def test_status_strings_and_null_arguments(built_lib):
     assert L.lg_get_tuning(None, None) == -1
     assert L.lg_set_tuning(None, None) == -1
     assert L.lg_autotune(None, None, None, None, None, None, None) == -1
+    assert L.lg_get_timeline(None, None, 0, None) == -1
 
 
 def test_python_mirror_struct_layout_matches_header(built_lib, tmp_path):

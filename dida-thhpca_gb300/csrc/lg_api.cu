@@ -71,12 +71,13 @@ struct lg_ctx {
     size_t cap = 0;        // solves
     size_t rot_n_cap = 0;  // rotation-log entries per solve it was sized for
   };
-  SolveLane lane[3];
+  SolveLane lane[4];
   int rot_cap = 0;
-  // extra solve streams (tune.solve_streams 2 and 3) and their ordering events
-  cudaStream_t side_stream = nullptr, third_stream = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join3 = nullptr;
-  cudaEvent_t ev_phase[3][3] = {};  // [Gram, eigensolve, vectors done][buffer set]
+  // extra solve streams (tune.solve_streams 2..4) and their ordering events
+  cudaStream_t side_stream = nullptr, third_stream = nullptr, fourth_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join3 = nullptr, ev_join4 = nullptr;
+  // [Gram, tridiagonalisation (or eigensolve), QL, vectors done][buffer set]
+  cudaEvent_t ev_phase[4][4] = {};
   // ln p bucketed records for the mixed-precision Gram
   float4* d_rec = nullptr;
   int* d_boff = nullptr;
@@ -255,12 +256,12 @@ double box_bound(float v) {
 }
 
 void release_streams(lg_ctx* c) {
-  for (cudaStream_t* sp : {&c->own_stream, &c->side_stream, &c->third_stream})
+  for (cudaStream_t* sp : {&c->own_stream, &c->side_stream, &c->third_stream, &c->fourth_stream})
     if (*sp) {
       cudaStreamDestroy(*sp);
       *sp = nullptr;
     }
-  for (cudaEvent_t* ep : {&c->ev_fork, &c->ev_join, &c->ev_join3})
+  for (cudaEvent_t* ep : {&c->ev_fork, &c->ev_join, &c->ev_join3, &c->ev_join4})
     if (*ep) {
       cudaEventDestroy(*ep);
       *ep = nullptr;
@@ -366,9 +367,11 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   bool made = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&c->third_stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&c->fourth_stream, cudaStreamNonBlocking) == cudaSuccess &&
               cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
               cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) == cudaSuccess &&
-              cudaEventCreateWithFlags(&c->ev_join3, cudaEventDisableTiming) == cudaSuccess;
+              cudaEventCreateWithFlags(&c->ev_join3, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&c->ev_join4, cudaEventDisableTiming) == cudaSuccess;
   for (auto& row : c->ev_phase)
     for (auto& e : row)
       made = made && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
@@ -811,7 +814,10 @@ int prepare_capacity(lg_ctx* c) {
   // test hook: a small log forces the overflow fallback path
   if (const char* env = getenv("LETKF_GB300_ROT_CAP")) c->rot_cap = std::max(1, atoi(env));
   const int nl = c->tune.solve_streams;
-  for (int li = 0; li < 3; ++li) {
+  // rotation log entries: (cos, sin) as two doubles, or two floats where only
+  // the FP32 vector kernel replays them (mixed precision)
+  const size_t rot_pairs_per_slot = g.precision == LG_PREC_MIXED ? 2 : 1;
+  for (int li = 0; li < 4; ++li) {
     lg_ctx::SolveLane& L = c->lane[li];
     const size_t cap = li < nl ? (size_t)c->chunk * levels : 0;
     if (L.cap >= cap && (cap > 0 || L.cap == 0) && L.rot_n_cap == (size_t)c->rot_cap) continue;
@@ -827,7 +833,8 @@ int prepare_capacity(lg_ctx* c) {
     if (c->use_eig2) {
       r |= dalloc(&L.tri, cap * lg::eig2_tri_doubles(k));
       r |= dalloc(&L.lam, cap * k);
-      r |= dalloc(&L.rot_cs, cap * (size_t)c->rot_cap);
+      r |= dalloc(&L.rot_cs, (cap * (size_t)c->rot_cap + rot_pairs_per_slot - 1) /
+                                 rot_pairs_per_slot);
       r |= dalloc(&L.rot_i, cap * (size_t)c->rot_cap);
       r |= dalloc(&L.rot_n, cap);
       r |= dalloc(&L.ovf_list, cap);
@@ -905,7 +912,7 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   // pipeline's other streams, the full-size one otherwise; per-solve streaming
   // where the column kernel does not apply.
   GramKind gram_kind = !lg::gram_col_supported(k)       ? GramKind::kStream
-                       : c->tune.solve_streams == 3 ? GramKind::kColumnLean
+                       : c->tune.solve_streams >= 3 ? GramKind::kColumnLean
                                                     : GramKind::kColumn;
   if (c->tune.gram_kernel == LG_GRAM_COLUMN && lg::gram_col_supported(k))
     gram_kind = GramKind::kColumn;
@@ -926,7 +933,12 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   //   3: a phase pipeline over three buffer sets -- Grams on one stream,
   //      tridiagonalisation + QL on st, vectors/update on a third, ordered by
   //      events -- so the FP64 eigensolve of chunk q runs beside the Gram of
-  //      chunk q+1 and the vector update of chunk q-1.
+  //      chunk q+1 and the vector update of chunk q-1;
+  //   4: the same with QL on a stream of its own and four buffer sets, so the
+  //      QL of chunk q (latency-bound: one lane per matrix, few warps per SM)
+  //      runs beside the tridiagonalisation of chunk q+1 (FP64-pipe-bound).
+  // A buffer set is reused by chunk q only after the vector update of chunk
+  // q - nl (the last reader of its Gram matrices and eigensolver scratch).
   // Per-chunk timing events (7 per chunk, each on its phase's stream): [0] Gram
   // start, [1] Gram end, [2] eigensolve start, [3] after tridiag, [4] after QL,
   // [5] vectors start, [6] vectors end.
@@ -934,15 +946,17 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   if (nl >= 2) {
     CK(cudaEventRecord(c->ev_fork, st));
     CK(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
-    if (nl == 3) CK(cudaStreamWaitEvent(c->third_stream, c->ev_fork, 0));
+    if (nl >= 3) CK(cudaStreamWaitEvent(c->third_stream, c->ev_fork, 0));
+    if (nl == 4) CK(cudaStreamWaitEvent(c->fourth_stream, c->ev_fork, 0));
   }
   const bool fp32_vec = g.precision == LG_PREC_MIXED;
   for (int q = 0; q < nchunks; ++q) {
     const int set = q % nl;
     lg_ctx::SolveLane& L = c->lane[set];
     cudaStream_t s = (nl == 2 && (q & 1)) ? c->side_stream : st;
-    cudaStream_t s_g = nl == 3 ? c->side_stream : s, s_e = s;
-    cudaStream_t s_v = nl == 3 ? c->third_stream : s;
+    cudaStream_t s_g = nl >= 3 ? c->side_stream : s, s_e = s;
+    cudaStream_t s_v = nl >= 3 ? c->third_stream : s;
+    cudaStream_t s_q = nl == 4 ? c->fourth_stream : s_e;
     cudaEvent_t* kv = &c->kev[7 * q];
     lg::SolveBatch b{};
     b.mode = 0;
@@ -952,7 +966,7 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     b.nsolves = b.ncols * levels;
     b.work = c->d_work;
     // Gram (phase pipeline: after the buffer set's previous vector update)
-    if (nl == 3 && q >= 3) CK(cudaStreamWaitEvent(s_g, c->ev_phase[2][set], 0));
+    if (nl >= 3 && q >= nl) CK(cudaStreamWaitEvent(s_g, c->ev_phase[3][set], 0));
     CK(record_event(kv[0], s_g));
     if (mixed_tc && (gram_kind == GramKind::kColumn || gram_kind == GramKind::kColumnLean))
       lg::launch_gram_col(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec,
@@ -965,19 +979,31 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
       lg::launch_gram64(geo, c->hx, c->lists, b, axb, L.C, L.t, s_g);
     CK(cudaMemsetAsync(L.ovf_n, 0, sizeof(int), s_g));
     CK(record_event(kv[1], s_g));
-    if (nl == 3) {
+    if (nl >= 3) {
       CK(cudaEventRecord(c->ev_phase[0][set], s_g));
       CK(cudaStreamWaitEvent(s_e, c->ev_phase[0][set], 0));
     }
     CK(record_event(kv[2], s_e));
     if (c->use_eig2) {
-      lg::launch_eig2(geo, b, L.C, L.t, xb, axb, xa, axa, L.tri, L.lam, L.rot_cs, L.rot_i,
-                      L.rot_n, c->rot_cap, L.ovf_list, L.ovf_n, c->d_status + 1, fp32_vec,
-                      c->tune.ql_warps, c->tune.vec_warps, lg::kEigTridiag | lg::kEigQL, s_e,
-                      kv[3], kv[4]);
-      if (nl == 3) {
+      if (s_q == s_e) {
+        lg::launch_eig2(geo, b, L.C, L.t, xb, axb, xa, axa, L.tri, L.lam, L.rot_cs, L.rot_i,
+                        L.rot_n, c->rot_cap, L.ovf_list, L.ovf_n, c->d_status + 1, fp32_vec,
+                        c->tune.ql_warps, c->tune.vec_warps, lg::kEigTridiag | lg::kEigQL, s_e,
+                        kv[3], kv[4]);
+      } else {
+        lg::launch_eig2(geo, b, L.C, L.t, xb, axb, xa, axa, L.tri, L.lam, L.rot_cs, L.rot_i,
+                        L.rot_n, c->rot_cap, L.ovf_list, L.ovf_n, c->d_status + 1, fp32_vec,
+                        c->tune.ql_warps, c->tune.vec_warps, lg::kEigTridiag, s_e, kv[3],
+                        nullptr);
         CK(cudaEventRecord(c->ev_phase[1][set], s_e));
-        CK(cudaStreamWaitEvent(s_v, c->ev_phase[1][set], 0));
+        CK(cudaStreamWaitEvent(s_q, c->ev_phase[1][set], 0));
+        lg::launch_eig2(geo, b, L.C, L.t, xb, axb, xa, axa, L.tri, L.lam, L.rot_cs, L.rot_i,
+                        L.rot_n, c->rot_cap, L.ovf_list, L.ovf_n, c->d_status + 1, fp32_vec,
+                        c->tune.ql_warps, c->tune.vec_warps, lg::kEigQL, s_q, nullptr, kv[4]);
+      }
+      if (nl >= 3) {
+        CK(cudaEventRecord(c->ev_phase[2][set], s_q));
+        CK(cudaStreamWaitEvent(s_v, c->ev_phase[2][set], 0));
       }
       CK(record_event(kv[5], s_v));
       lg::launch_eig2(geo, b, L.C, L.t, xb, axb, xa, axa, L.tri, L.lam, L.rot_cs, L.rot_i,
@@ -995,23 +1021,27 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
                            c->d_status + 1, s_e);
       CK(record_event(kv[3], s_e));
       CK(record_event(kv[4], s_e));
-      if (nl == 3) {
-        CK(cudaEventRecord(c->ev_phase[1][set], s_e));
-        CK(cudaStreamWaitEvent(s_v, c->ev_phase[1][set], 0));
+      if (nl >= 3) {
+        CK(cudaEventRecord(c->ev_phase[2][set], s_e));
+        CK(cudaStreamWaitEvent(s_v, c->ev_phase[2][set], 0));
       }
       CK(record_event(kv[5], s_v));
       launches += 1;
     }
     CK(record_event(kv[6], s_v));
-    if (nl == 3) CK(cudaEventRecord(c->ev_phase[2][set], s_v));
+    if (nl >= 3) CK(cudaEventRecord(c->ev_phase[3][set], s_v));
     launches += 1;
   }
   if (nl >= 2) {
     CK(cudaEventRecord(c->ev_join, c->side_stream));
     CK(cudaStreamWaitEvent(st, c->ev_join, 0));
-    if (nl == 3) {
+    if (nl >= 3) {
       CK(cudaEventRecord(c->ev_join3, c->third_stream));
       CK(cudaStreamWaitEvent(st, c->ev_join3, 0));
+    }
+    if (nl == 4) {
+      CK(cudaEventRecord(c->ev_join4, c->fourth_stream));
+      CK(cudaStreamWaitEvent(st, c->ev_join4, 0));
     }
   }
   CK(record_event(c->ev[3], st));
@@ -1227,7 +1257,7 @@ int lg_set_tuning(lg_ctx* c, const lg_tuning* t) {
   if (t->chunk_mb < 16 || t->chunk_mb > 65536 || t->gram_kernel < LG_GRAM_AUTO ||
       t->gram_kernel > LG_GRAM_COLUMN_LEAN || t->lnp_buckets < 8 || t->lnp_buckets > 1024 ||
       t->ql_warps < 1 || t->ql_warps > 6 || t->vec_warps < 1 || t->vec_warps > 8 ||
-      t->solve_streams < 1 || t->solve_streams > 3 || t->gram_ctas < 0 || t->gram_ctas > 4096)
+      t->solve_streams < 1 || t->solve_streams > 4 || t->gram_ctas < 0 || t->gram_ctas > 4096)
     return LG_ERR_ARG;
   c->tune = *t;
   c->capacity_ready = false;  // chunk size and bucket count size buffers
@@ -1245,7 +1275,7 @@ int lg_autotune(lg_ctx* c, const double* xb, const double* axb, double* xa, doub
   lg_tuning cur = c->tune;
   if (cur.gram_kernel == LG_GRAM_AUTO)
     cur.gram_kernel = !lg::gram_col_supported(g.ens) ? LG_GRAM_STREAM
-                      : cur.solve_streams == 3          ? LG_GRAM_COLUMN_LEAN
+                      : cur.solve_streams >= 3          ? LG_GRAM_COLUMN_LEAN
                                                         : LG_GRAM_COLUMN;
   // one untimed analysis (buffer sizing, graph capture), then the faster of two
   auto measure = [&](const lg_tuning& t, double* ms) -> int {
@@ -1282,7 +1312,7 @@ int lg_autotune(lg_ctx* c, const double* xb, const double* axb, double* xa, doub
     }
     return LG_OK;
   };
-  if ((r = try_param(&lg_tuning::solve_streams, {1, 2, 3})) != LG_OK) return r;
+  if ((r = try_param(&lg_tuning::solve_streams, {1, 2, 3, 4})) != LG_OK) return r;
   if ((r = try_param(&lg_tuning::chunk_mb, {256, 512, 1024, 2048, 4096})) != LG_OK) return r;
   if (mixed) {
     if (lg::gram_col_supported(g.ens)) {

@@ -206,7 +206,7 @@ int lg_get_timeline(const lg_ctx* ctx, float* ms, int cap, int* nchunks);
  * change the FP32 summation order.  No reference counterpart: the reference
  * has no GPU path to tune. */
 #define LG_GRAM_AUTO 0   /* column groups where supported (the lean variant with three
-                            solve streams), else per-solve streaming */
+                            or four solve streams), else per-solve streaming */
 #define LG_GRAM_COLUMN 1 /* one CTA per SM over (column, 8 levels) items, rows read once per group */
 #define LG_GRAM_STREAM 2 /* one CTA per solve streaming its ln p window of records */
 #define LG_GRAM_QUEUE 3  /* one CTA per solve compacting non-zero weights through a queue */
@@ -222,7 +222,8 @@ typedef struct lg_tuning {
   int vec_warps;   /* warps per block of the vector/update kernel, 1..8 */
   int solve_streams; /* 1; 2: chunks alternate between two streams with their own scratch;
                         3: phase pipeline (Grams, eigensolves, vector updates on three
-                        streams, three buffer sets) */
+                        streams, three buffer sets); 4: as 3 with tridiagonalisation
+                        and QL on separate streams, four buffer sets */
   int gram_ctas;   /* persistent CTAs of the column Gram, 0 = one per SM; fewer leave
                       whole SMs to the eigensolve beside it */
   double ms;       /* device time of one analysis with these settings (lg_autotune) */

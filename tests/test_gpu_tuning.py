@@ -37,21 +37,30 @@ def test_set_tuning_validates_and_round_trips():
     t2 = ctx.tuning()
     assert (t2["chunk_mb"], t2["ql_warps"], t2["vec_warps"], t2["lnp_buckets"]) == (64, 2, 8, 32)
     for bad in ({"chunk_mb": 1}, {"ql_warps": 0}, {"ql_warps": 7}, {"vec_warps": 9},
-                {"lnp_buckets": 4}, {"gram_kernel": 9}, {"solve_streams": 4}, {"gram_ctas": -1}):
+                {"lnp_buckets": 4}, {"gram_kernel": 9}, {"solve_streams": 5}, {"gram_ctas": -1}):
         with pytest.raises(RuntimeError, match="LG_ERR_ARG"):
             ctx.set_tuning(**bad)
     ctx.letkf_final()
 
 
-def test_fp64_analysis_is_bit_identical_under_every_setting():
+def test_fp64_analysis_is_bit_identical_under_every_setting(monkeypatch):
     import letkf_gb300 as lg
     cfg, w = _workload("tiny3d")
     ctx = lg.Letkf(cfg)
     ctx.set_obs(w.obs)
     ref = None
+    # "mb1": 1 MiB chunks (LETKF_GB300_CHUNK_MB), 11 chunks of 64 columns, so
+    # every schedule reuses its buffer sets
     for kw in ({}, {"chunk_mb": 16}, {"ql_warps": 4, "vec_warps": 2}, {"vec_warps": 8},
                {"solve_streams": 2, "chunk_mb": 16}, {"solve_streams": 3, "chunk_mb": 16},
+               {"solve_streams": 4, "chunk_mb": 16}, {"solve_streams": 2, "mb1": 1},
+               {"solve_streams": 3, "mb1": 1}, {"solve_streams": 4, "mb1": 1},
                {"solve_streams": 1}):
+        kw = dict(kw)
+        if kw.pop("mb1", 0):
+            monkeypatch.setenv("LETKF_GB300_CHUNK_MB", "1")
+        else:
+            monkeypatch.delenv("LETKF_GB300_CHUNK_MB", raising=False)
         ctx.set_tuning(**kw)
         xa = np.zeros_like(w.xb)
         axa = np.zeros_like(w.axb)

@@ -298,6 +298,10 @@ def main():
     iso = ctx.stats()
     if tuning["solve_streams"] != 1:
         ctx.set_tuning(solve_streams=tuning["solve_streams"])
+    # the analysis is finite everywhere it writes (interior points)
+    h = cfg.halo
+    if not (bool(torch.isfinite(xa[h:-h, h:-h]).all()) and bool(torch.isfinite(axa[h:-h, h:-h]).all())):
+        raise RuntimeError("non-finite analysis values")
 
     # roofline of the dominant kernel: algorithmic FLOPs of its launches in one
     # analysis over the sum of their event-timed durations

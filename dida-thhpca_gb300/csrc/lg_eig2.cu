@@ -25,7 +25,8 @@
 //
 // W and V are never formed; the cost per matrix is the reduction (2k^3/3 FMA)
 // plus O(k^2) per vector.  A matrix whose QL needs more rotations than the log
-// holds is flagged and redone by eig_apply_kernel (lg_eig.cu).
+// holds, or (mixed path) whose reduction has an h beyond the FP32 reflector
+// range, is flagged and redone in FP64 by eig_apply_kernel (lg_eig.cu).
 #include <float.h>
 
 #include <algorithm>
@@ -44,10 +45,12 @@ __device__ inline size_t uoff(int i) { return (size_t)i * (i - 1) / 2; }   // ro
 // scratch layout per solve: D[n] | E[n] | H[n] | U[n(n-1)/2]
 //
 // The matrix is held as its packed lower triangle, row j at j(j+1)/2 (16.6 KB for
-// 64 members, so 13 warps fit an SM).  Every shared-memory access pattern below
-// is free of bank conflicts within a half-warp: consecutive elements of a row,
-// the same column of consecutive rows j (offsets j(j+1)/2 + c, and j(j+1)/2 is a
-// permutation modulo 16 over any 16 consecutive j), or a broadcast.  The kernel
+// 64 members, so 13 warps fit an SM).  The shared-memory access patterns below
+// are free of bank conflicts within a half-warp -- consecutive elements of a
+// row, the same column of consecutive rows j (offsets j(j+1)/2 + c, and
+// j(j+1)/2 is a permutation modulo 16 over any 16 consecutive j), or a
+// broadcast -- except the column runs of the split rows in the matrix-vector
+// product, where a few conflicts cost less than idle FP64 lanes.  The kernel
 // is bound by the FP64 pipe, so the instruction count is what is minimised: the
 // reflector needs no pre-scaling unless the row's squared norm leaves
 // [2^-900, 2^900], the matrix-vector product runs every lane over the same
@@ -71,8 +74,21 @@ __device__ inline double rcp_nr(double x) {
 __device__ inline int dexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
 
 // u32 = 1 (mixed path): the reflectors are written in FP32 for the FP32 vector
-// kernel -- U as floats at the start of the U region and 1/h as floats after
-// them -- so that kernel converts nothing; the double H is kept for reference.
+// kernel, normalised as v = u / sqrt(h) (P = I - v v^T, |v|^2 = 2 whatever the
+// size of h, so a rounding-level row of a low-rank matrix neither overflows nor
+// underflows in FP32), at the start of the U region, followed by one float per
+// step: 1 where the step has a reflector, 0 where it has none.  A matrix with
+// an h outside [2^-200, 2^200] is marked by H[0] = 1 (the QL kernel passes it
+// to the FP64 fallback solver); the double H is kept for reference.
+__device__ inline float rsqrt_f32_of(double h) {
+  // 1/sqrt(h) for a normal h in [2^-200, 2^200]: h = m 2^e2 with e2 even and m
+  // in [1, 4) (exponent bits only), then rsqrtf(m) 2^(-e2/2)
+  const int hb = __double2hiint(h);
+  const int e2 = (((hb >> 20) & 0x7ff) - 1023) & ~1;
+  const double m = __hiloint2double(hb - (e2 << 20), __double2loint(h));
+  return rsqrtf((float)m) * __int_as_float((127 - e2 / 2) << 23);
+}
+
 __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const double* Cin,
                                                      double* tri, int u32) {
   const int s = blockIdx.x;
@@ -111,11 +127,12 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
     return v;
   };
   float* U32 = reinterpret_cast<float*>(U);
-  float* Hinv32 = U32 + (size_t)n * (n - 1) / 2;
+  float* Act32 = U32 + (size_t)n * (n - 1) / 2;
+  bool extreme = false;  // some h outside the FP32 reflector range
   for (int i = n - 1; i >= 1; --i) {
     const int l = i - 1;
     double* row = P + tri_idx(i);  // u: row i, columns 0..l
-    double h = 0.0, ei, hinv = 0.0;
+    double h = 0.0, ei;
     if (l > 0) {
       double ss = 0.0;
       for (int c = lane; c <= l; c += 32) ss = fma(row[c], row[c], ss);
@@ -148,16 +165,23 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
         __syncwarp();
         if (lane == 0) row[l] = f - gg;
         __syncwarp();
-        // p = A u / h, lane j over row j: columns c <= j from row j, c > j from
-        // column j (the same trip count on every lane)
+        // p = A u / h over the R = l + 1 rows; element (j, c) is read from row j
+        // for c <= j and from row c (column j) for c > j.  With R > 32, lane j
+        // first takes the whole row j < 32.  The remaining r rows are split
+        // over groups of f lanes (f the largest power of two with r f <= 32),
+        // each lane summing a run of ceil(R / f) columns, and the group sums
+        // meet by shuffles: the FP64 pipe then issues about R + ceil(R / f) +
+        // log2 f instructions instead of R per 32 rows.
         const double inv_h = rcp_nr(h);
-        hinv = inv_h;
         double fs = 0.0;
-        for (int j = lane; j <= l; j += 32) {
+        const int R = l + 1;
+        const int nfull = R > 32 ? 32 : 0;
+        if (nfull) {
+          const int j = lane;
           const int tj = tri_idx(j);
           double gj = 0.0;
           int tc = 0;  // c(c+1)/2
-          for (int c = 0; c <= l; ++c) {
+          for (int c = 0; c < R; ++c) {
             const int off = (c <= j) ? tj + c : tc + j;
             gj = fma(P[off], row[c], gj);
             tc += c + 1;
@@ -166,6 +190,32 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
           q[j] = pj;
           fs = fma(pj, row[j], fs);
         }
+        {
+          const int r = R - nfull;                     // 1..32
+          const int lf = 31 - __clz(32 / r);           // f = 2^lf, r f <= 32
+          const int f = 1 << lf;
+          const int cl = (R + f - 1) >> lf;            // columns per lane
+          const int ri = lane >> lf, pi = lane & (f - 1);
+          const bool act = ri < r;
+          const int j = nfull + (act ? ri : 0);
+          const int c0 = act ? min(R, pi * cl) : 0;
+          const int c1 = act ? min(R, c0 + cl) : 0;
+          const int tj = tri_idx(j);
+          double gj = 0.0;
+          int tc = tri_idx(c0);
+          for (int c = c0; c < c1; ++c) {
+            const int off = (c <= j) ? tj + c : tc + j;
+            gj = fma(P[off], row[c], gj);
+            tc += c + 1;
+          }
+          for (int o = f >> 1; o > 0; o >>= 1) gj += __shfl_xor_sync(0xffffffffu, gj, o);
+          const double pj = gj * inv_h;
+          if (act && pi == 0) {
+            q[j] = pj;
+            fs = fma(pj, row[j], fs);
+          }
+        }
+        __syncwarp();  // q[j] of a split row was written by its group's first lane
         const double kq = wsum(fs) * (0.5 * inv_h);
         for (int j = lane; j <= l; j += 32) q[j] = fma(-kq, row[j], q[j]);
         __syncwarp();
@@ -193,8 +243,12 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
     }
     // reflector of step i: u = row i (scaled), h
     if (u32) {
-      for (int c = lane; c < i; c += 32) U32[e2::uoff(i) + c] = (float)row[c];
-      if (lane == 0) Hinv32[i] = (float)hinv;
+      const int eh = dexp(h);
+      const bool in_range = eh >= 1023 - 200 && eh <= 1023 + 200;
+      extreme |= h != 0.0 && !in_range;
+      const float sv = in_range ? rsqrt_f32_of(h) : 0.0f;
+      for (int c = lane; c < i; c += 32) U32[e2::uoff(i) + c] = (float)row[c] * sv;
+      if (lane == 0) Act32[i] = in_range ? 1.0f : 0.0f;
     } else {
       for (int c = lane; c < i; c += 32) U[e2::uoff(i) + c] = row[c];
     }
@@ -206,9 +260,9 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
   }
   for (int i = lane; i < n; i += 32) D[i] = P[tri_idx(i) + i];
   if (lane == 0) {
-    H[0] = 0.0;
+    H[0] = extreme ? 1.0 : 0.0;
     E[0] = 0.0;
-    if (u32) Hinv32[0] = 0.0f;
+    if (u32) Act32[0] = 0.0f;
   }
 }
 
@@ -238,8 +292,10 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
 #define DD(i) d[(i) * 32 + lane]
 #define EE(i) e[(i) * 32 + lane]
   const bool live = s < nsolves;
+  bool marked = false;  // an h outside the FP32 reflector range (mixed path): FP64 fallback
   if (live) {
     const double* T = tri + (size_t)s * e2::tri_stride(n);
+    marked = T[2 * n] != 0.0;
     for (int i = 0; i < n; ++i) {
       DD(i) = T[i];
       EE(i) = (i + 1 < n) ? T[n + i + 1] : 0.0;  // e[i] = T(i, i+1)
@@ -261,7 +317,7 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
   // The lanes of a warp run their QL sweeps in step: one sweep per pass of the
   // loop below, from the lane's first split m below l up to l, as in tql2.
   int l = 0, iter = 0, nrot = 0;
-  bool fail = false, over = false, done = !live;
+  bool fail = false, over = marked, done = !live || marked;
   while (true) {
     int m = n - 1;
     if (!done) {
@@ -409,14 +465,12 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
     // y = Q^T x = P_1 ... P_{n-1} x  (P_{n-1} first)
     if constexpr (kF32) {
       const float* U32 = reinterpret_cast<const float*>(T + 3 * n);
-      const float* Hinv32 = U32 + (size_t)n * (n - 1) / 2;
+      const float* Act32 = U32 + (size_t)n * (n - 1) / 2;
       for (int i = n - 1; i >= 1; --i) {
-        const float hinv = Hinv32[i];
-        if (hinv == 0.0f) continue;
-        const float* u = U32 + e2::uoff(i);
+        if (Act32[i] == 0.0f) continue;
+        const float* u = U32 + e2::uoff(i);  // v = u / sqrt(h): P = I - v v^T
         float dot = 0.0f;
         for (int kk = 0; kk < i; ++kk) dot += u[kk] * YY(kk);
-        dot *= hinv;
         for (int kk = 0; kk < i; ++kk) YY(kk) -= u[kk] * dot;
       }
     } else {
@@ -486,14 +540,12 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
     // y = Q y = P_{n-1} ... P_1 y  (P_1 first)
     if constexpr (kF32) {
       const float* U32 = reinterpret_cast<const float*>(T + 3 * n);
-      const float* Hinv32 = U32 + (size_t)n * (n - 1) / 2;
+      const float* Act32 = U32 + (size_t)n * (n - 1) / 2;
       for (int i = 1; i < n; ++i) {
-        const float hinv = Hinv32[i];
-        if (hinv == 0.0f) continue;
+        if (Act32[i] == 0.0f) continue;
         const float* u = U32 + e2::uoff(i);
         float dot = 0.0f;
         for (int kk = 0; kk < i; ++kk) dot += u[kk] * YY(kk);
-        dot *= hinv;
         for (int kk = 0; kk < i; ++kk) YY(kk) -= u[kk] * dot;
       }
     } else {

@@ -13,9 +13,15 @@ TOL_INCREMENT = 1e-4
 
 
 def increment_rel_rms(cfg, w, got, ref):
+    """Per-variable relative RMS of the increment difference.  A non-finite
+    analysis value anywhere in the interior makes every entry inf, so that a
+    comparison against a tolerance fails (a NaN would compare false and slip
+    through max())."""
     h = cfg.halo
     xa, axa = got
     xa_o, axa_o = ref
+    if not (np.all(np.isfinite(xa[h:-h, h:-h])) and np.all(np.isfinite(axa[h:-h, h:-h]))):
+        return {v: float("inf") for v in cfg.var_names}
     bg = (w.xb + w.axb[..., None])[h:-h, h:-h]
     inc_g = (xa + axa[..., None])[h:-h, h:-h] - bg
     inc_o = (xa_o + axa_o[..., None])[h:-h, h:-h] - bg
@@ -24,7 +30,8 @@ def increment_rel_rms(cfg, w, got, ref):
     for v, lv in zip(cfg.var_names, cfg.var_lev):
         sl = slice(r0, r0 + lv)
         d = inc_g[:, :, sl] - inc_o[:, :, sl]
-        out[v] = float(np.sqrt(np.mean(d ** 2)) / np.sqrt(np.mean(inc_o[:, :, sl] ** 2)))
+        val = float(np.sqrt(np.mean(d ** 2)) / np.sqrt(np.mean(inc_o[:, :, sl] ** 2)))
+        out[v] = val if np.isfinite(val) else float("inf")
         r0 += lv
     return out
 
@@ -148,6 +155,8 @@ def test_mixed_schedules_agree_bit_for_bit(monkeypatch):
         axa = np.zeros_like(w.axb)
         ctx.letkf_run(0, w.xb, w.axb, xa, axa)
         assert ctx.stats()["n_chunks"] > 4 * nl
+        h = cfg.halo
+        assert np.all(np.isfinite(xa[h:-h, h:-h])) and np.all(np.isfinite(axa[h:-h, h:-h])), nl
         if ref is None:
             ref = (xa, axa)
         else:

@@ -86,7 +86,7 @@ struct lg_ctx {
   double lnp_span = 1.0;
   int boff_nb = 0;  // bucket count d_boff was sized for
   // launch shapes and bucket boundaries (lg_set_tuning / lg_autotune)
-  lg_tuning tune{1024, LG_GRAM_AUTO, 128, 1, 4, 3, 0, 0.0};
+  lg_tuning tune{1024, LG_GRAM_AUTO, 128, 1, 4, 4, 0, 0.0};
   // status words: [0] err, [1] eig_fail
   int* d_status = nullptr;
   unsigned long long* d_band = nullptr;
@@ -364,10 +364,29 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   lg_ctx* c = new lg_ctx();
   c->cfg = g;
   cudaGetDevice(&c->dev);
+  // Scheduling priorities of the solve streams (Gram, vector update, QL): a
+  // level 0 (lowest, the default stream's), 1 or 2 (highest) each.  Pending
+  // blocks of a higher-priority stream are dispatched first when SM resources
+  // free up; the captured graph keeps them (per-node priorities).  Default:
+  // the short vector updates (which free a buffer set for the next Gram) and
+  // the latency-bound QL first, the Grams and tridiagonalisations (on the
+  // caller's stream) filling the rest; LETKF_GB300_PRIO="g,v,q" overrides.
+  int plev[3] = {0, 2, 2};
+  if (const char* e = getenv("LETKF_GB300_PRIO"))
+    sscanf(e, "%d,%d,%d", &plev[0], &plev[1], &plev[2]);
+  int p_least = 0, p_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&p_least, &p_greatest);
+  auto prio = [&](int lv) {
+    lv = std::max(0, std::min(2, lv));
+    return lv == 0 ? p_least : lv == 2 ? p_greatest : (p_least + p_greatest) / 2;
+  };
   bool made = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&c->third_stream, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&c->fourth_stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithPriority(&c->side_stream, cudaStreamNonBlocking, prio(plev[0])) ==
+                  cudaSuccess &&
+              cudaStreamCreateWithPriority(&c->third_stream, cudaStreamNonBlocking, prio(plev[1])) ==
+                  cudaSuccess &&
+              cudaStreamCreateWithPriority(&c->fourth_stream, cudaStreamNonBlocking, prio(plev[2])) ==
+                  cudaSuccess &&
               cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
               cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) == cudaSuccess &&
               cudaEventCreateWithFlags(&c->ev_join3, cudaEventDisableTiming) == cudaSuccess &&
@@ -1079,7 +1098,9 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
       if (ok) er = enqueue_analysis(c, xb, axb, xa, axa, st, &launches);
       const cudaError_t ee = ok ? cudaStreamEndCapture(st, &graph) : cudaErrorUnknown;
       ok = ok && er == LG_OK && ee == cudaSuccess && graph != nullptr;
-      if (ok) ok = cudaGraphInstantiate(&c->graph_exec, graph, 0) == cudaSuccess;
+      if (ok)
+        ok = cudaGraphInstantiateWithFlags(&c->graph_exec, graph,
+                                           cudaGraphInstantiateFlagUseNodePriority) == cudaSuccess;
       if (graph) cudaGraphDestroy(graph);
       if (!ok) {
         cudaGetLastError();

@@ -181,8 +181,11 @@ __device__ inline void item_levels(const SolveBatch& b, int item, int& col, int&
 
 // kRing: stages of records and ensemble rows in flight; kOps: operand buffers
 // between the converter warps and the MMA warp.  <6, 4> fills an SM's shared
-// memory (one CTA per SM, 178 KB); <3, 3> leaves ~120 KB of it to kernels of the
-// other solve streams (tridiagonalisation, QL) running beside it.
+// memory (one CTA per SM, 174 KB); <2, 3> (90 KB; the epilogue's accumulator
+// copy needs three operand buffers) leaves ~138 KB of it to kernels of the
+// other solve streams (tridiagonalisation, QL) running beside it: the
+// tridiagonalisation is latency-bound below about two warps per SM
+// sub-partition, so every 17 KB it gets back is a matrix in flight.
 template <int kRing, int kOps>
 __global__ void __launch_bounds__(colk::kThreads, 1)
     gram_col_kernel(Geometry g, HxDev hx, ListDev l, SolveBatch b, const double* axb,
@@ -536,9 +539,9 @@ void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const
   const int nitems = b.ncols * ngrp;
   const int grid = std::min(nitems, ctas > 0 ? ctas : sms);
   if (lean) {
-    constexpr int bytes = colk::Layout<3, 3>::kBytes;
-    cudaFuncSetAttribute(gram_col_kernel<3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    gram_col_kernel<3, 3><<<grid, colk::kThreads, bytes, stream>>>(g, hx, l, b, axb, C, t, err, rec);
+    constexpr int bytes = colk::Layout<2, 3>::kBytes;
+    cudaFuncSetAttribute(gram_col_kernel<2, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    gram_col_kernel<2, 3><<<grid, colk::kThreads, bytes, stream>>>(g, hx, l, b, axb, C, t, err, rec);
   } else {
     constexpr int bytes = colk::Layout<6, 4>::kBytes;
     cudaFuncSetAttribute(gram_col_kernel<6, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);

@@ -65,7 +65,7 @@ struct Layout {
   static constexpr int kOffRec = kOffOps + kOps * kOpBytes;
   static constexpr int kOffW = kOffRec + kRing * kRows * 16;
   static constexpr int kBytes = kOffW + 8 * 2 * kG * 16 * 4;
-  static_assert(128 * kDS * 4 <= kOps * kOpBytes, "accumulator copy must fit the operand buffers");
+  static_assert(64 * kDS * 4 <= kOps * kOpBytes, "epilogue staging must fit the operand buffers");
 };
 
 // instruction descriptor: kind::f16, BF16 A/B, FP32 D, K-major A and B, M = 128, N = 64
@@ -181,13 +181,15 @@ __device__ inline void item_levels(const SolveBatch& b, int item, int& col, int&
 
 // kRing: stages of records and ensemble rows in flight; kOps: operand buffers
 // between the converter warps and the MMA warp.  <6, 4> fills an SM's shared
-// memory (one CTA per SM, 174 KB); <2, 3> (90 KB; the epilogue's accumulator
-// copy needs three operand buffers) leaves ~138 KB of it to kernels of the
+// memory (one CTA per SM, 174 KB); <2, 2> (74 KB) leaves ~154 KB of it to kernels of the
 // other solve streams (tridiagonalisation, QL) running beside it: the
 // tridiagonalisation is latency-bound below about two warps per SM
 // sub-partition, so every 17 KB it gets back is a matrix in flight.
+// 128 registers a thread (40 K of the SM's 64 K, launched as 320 threads): the
+// compiler would otherwise take ~164 for the unrolled epilogue and leave the
+// FP64 kernels beside the Gram short of registers.
 template <int kRing, int kOps>
-__global__ void __launch_bounds__(colk::kThreads, 1)
+__global__ void __maxnreg__(128)
     gram_col_kernel(Geometry g, HxDev hx, ListDev l, SolveBatch b, const double* axb,
                     double* Cout, double* tout, int* err, RecDev rec) {
   using namespace colk;
@@ -472,7 +474,16 @@ __global__ void __launch_bounds__(colk::kThreads, 1)
       conv_sync();
       if (!s_go) break;
       tc::fence_after();
-      float* D = reinterpret_cast<float*>(ops);
+      // Epilogue in one 64 x 64 FP32 staging copy S (row stride kDS) in the
+      // operand buffers: C[i][j] = hi[i][j] + (lo[i][j] + lo[j][i]), where hi is
+      // accumulator row i (TMEM lanes 0..63) and lo row 64 + i.  The lo rows go
+      // to S first; then each hi-row thread folds its row's lower triangle into
+      // S in place -- it reads S[i][j] (its own row) and S[j][i] for j < i (the
+      // upper triangle of row j, which no thread writes) -- and C is written
+      // from the lower triangle.  A warp reads TMEM lanes 32 (warp % 4) ..;
+      // warps 0-3 take columns 0..31, warps 4-7 columns 32..63.
+      float* S = reinterpret_cast<float*>(ops);
+      const int wq = warp & 3, cb = (warp >> 2) * 32;
       const int levels = b.levels;
       for (int lv = 0; lv < G; ++lv) {
         const size_t s = (size_t)(col - b.first_col) * levels + (kk0 - 1 + lv);
@@ -483,13 +494,15 @@ __global__ void __launch_bounds__(colk::kThreads, 1)
           for (int i = tid; i < k; i += kConv) t[i] = 0.0;
           continue;
         }
-        if (warp < 4) {
+        const uint32_t taddr = tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(lv * kN + cb);
+        if (wq >= 2) {
+          const int r = (wq - 2) * 32 + lane;
 #pragma unroll
-          for (int c0 = 0; c0 < kN; c0 += 16) {
+          for (int c0 = 0; c0 < 32; c0 += 16) {
             float v[16];
-            tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(lv * kN + c0), v);
+            tc::tmem_ld16(taddr + (uint32_t)c0, v);
 #pragma unroll
-            for (int i = 0; i < 16; ++i) D[(warp * 32 + lane) * kDS + c0 + i] = v[i];
+            for (int i = 0; i < 16; ++i) S[r * kDS + cb + c0 + i] = v[i];
           }
         }
         float tv = 0.0f;
@@ -498,9 +511,23 @@ __global__ void __launch_bounds__(colk::kThreads, 1)
           if (u == lv) tv = tacc[u];
         s_t[q][m] = tv;
         conv_sync();
+        if (wq < 2) {
+          const int i = wq * 32 + lane;
+#pragma unroll
+          for (int c0 = 0; c0 < 32; c0 += 16) {
+            float v[16];
+            tc::tmem_ld16(taddr + (uint32_t)c0, v);
+#pragma unroll
+            for (int ii = 0; ii < 16; ++ii) {
+              const int j = cb + c0 + ii;
+              if (j <= i) S[i * kDS + j] = v[ii] + (S[i * kDS + j] + S[j * kDS + i]);
+            }
+          }
+        }
+        conv_sync();
         for (int idx = tid; idx < k * k; idx += kConv) {
           const int i = idx % k, j = idx / k;
-          C[idx] = (double)(D[i * kDS + j] + (D[(64 + i) * kDS + j] + D[(64 + j) * kDS + i]));
+          C[idx] = (double)(i >= j ? S[i * kDS + j] : S[j * kDS + i]);
         }
         if (tid < k) t[tid] = (double)((s_t[0][tid] + s_t[1][tid]) + (s_t[2][tid] + s_t[3][tid]));
         conv_sync();
@@ -539,9 +566,9 @@ void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const
   const int nitems = b.ncols * ngrp;
   const int grid = std::min(nitems, ctas > 0 ? ctas : sms);
   if (lean) {
-    constexpr int bytes = colk::Layout<2, 3>::kBytes;
-    cudaFuncSetAttribute(gram_col_kernel<2, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    gram_col_kernel<2, 3><<<grid, colk::kThreads, bytes, stream>>>(g, hx, l, b, axb, C, t, err, rec);
+    constexpr int bytes = colk::Layout<2, 2>::kBytes;
+    cudaFuncSetAttribute(gram_col_kernel<2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    gram_col_kernel<2, 2><<<grid, colk::kThreads, bytes, stream>>>(g, hx, l, b, axb, C, t, err, rec);
   } else {
     constexpr int bytes = colk::Layout<6, 4>::kBytes;
     cudaFuncSetAttribute(gram_col_kernel<6, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);

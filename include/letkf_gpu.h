@@ -210,7 +210,7 @@ int lg_get_timeline(const lg_ctx* ctx, float* ms, int cap, int* nchunks);
 #define LG_GRAM_COLUMN 1 /* one CTA per SM over (column, 8 levels) items, rows read once per group */
 #define LG_GRAM_STREAM 2 /* one CTA per solve streaming its ln p window of records */
 #define LG_GRAM_QUEUE 3  /* one CTA per solve compacting non-zero weights through a queue */
-#define LG_GRAM_COLUMN_LEAN 4 /* as LG_GRAM_COLUMN with a 2-stage ring (90 KB of shared
+#define LG_GRAM_COLUMN_LEAN 4 /* as LG_GRAM_COLUMN with a 2-stage ring (74 KB of shared
                                  memory), leaving room on each SM for other streams' kernels */
 
 typedef struct lg_tuning {

@@ -37,12 +37,13 @@ for p in (ROOT, PKG):
 
 METRIC = "LETKF grid columns/s, mixed vs plain FP64 on one GB300 at <=1e-4 rel RMS"
 UNIT = "columns/s"
-# DRAM bytes (read + write) per solve of the solve-phase kernels, from an ncu
-# capture of the 180x90x32 / N=64 / 2.5e5-observation workload in 256 MiB
-# chunks (8192 solves per launch; profiles/traffic_solve_kernels_prof.md).
+# DRAM bytes (read + write) per solve of the solve-phase kernels, from a
+# one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# 180x90x32 / N=64 / 2.5e5-observation workload in 256 MiB chunks (8192
+# solves per launch); the traffic grows in proportion to the solves.
 PROFILED_DRAM_BYTES_PER_SOLVE = {
-    "tridiag": 31.8e3,
-    "gram": 29.6e3,
+    "tridiag": 25.7e3,
+    "gram": 29.3e3,
 }
 
 

@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg3")
     ap.add_argument("--precision", default=None, choices=[None, "fp64", "mixed"])
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the bounded oracle sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -390,8 +390,11 @@ def main():
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             ctx.set_obs(w.obs)
+            t1 = time.perf_counter()
             ctx.letkf_run(0, nxb, naxb, nxa, naxa)
             ts.append(time.perf_counter() - t0)
+            print("e2e step: lg_set_obs %.1f ms, lg_run %.1f ms (device analysis %.1f ms)" % (
+                1e3 * (t1 - t0), 1e3 * (ts[-1] - (t1 - t0)), ctx.stats()["ms_total"]), file=sys.stderr)
         o = w.obs
         h2d = nxb.nbytes + naxb.nbytes + sum(a.nbytes for a in (o.type, o.lat, o.lon, o.ph, o.yo, o.rinv))
         h = cfg.halo

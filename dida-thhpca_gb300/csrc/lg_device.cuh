@@ -58,4 +58,33 @@ __device__ inline double latlon_dist_pre(double cx1, double sx1, double yr1, dou
 
 __device__ inline unsigned lane_id() { return threadIdx.x & 31u; }
 
+// Conversions between double and float by integer operations on the bit
+// fields, so that they do not issue on the FP64 pipe (a warp instruction per
+// ~16 cycles per SM on GB300, which the FP64 kernels beside them need).
+// Finite inputs only; values below the float normal range become (signed) zero.
+
+// double -> float, rounded to nearest, ties to even
+__device__ inline float d2f_bits(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 of 52 mantissa bits
+  const unsigned rest = lo & 0x1fffffffu;                  // the 29 dropped bits
+  unsigned bits = ((unsigned)e << 23) | m;
+  bits += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;  // may carry into e
+  return __uint_as_float(sign | bits);
+}
+
+// float -> double (exact)
+__device__ inline double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u;
+  const unsigned ef = (u >> 23) & 0xffu;
+  if (ef == 0u) return __hiloint2double((int)sign, 0);
+  const unsigned hi = sign | ((ef + (1023u - 127u)) << 20) | ((u & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)((u & 7u) << 29));
+}
+
 }  // namespace lg

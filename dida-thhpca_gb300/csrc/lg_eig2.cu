@@ -86,7 +86,7 @@ __device__ inline float rsqrt_f32_of(double h) {
   const int hb = __double2hiint(h);
   const int e2 = (((hb >> 20) & 0x7ff) - 1023) & ~1;
   const double m = __hiloint2double(hb - (e2 << 20), __double2loint(h));
-  return rsqrtf((float)m) * __int_as_float((127 - e2 / 2) << 23);
+  return rsqrtf(d2f_bits(m)) * __int_as_float((127 - e2 / 2) << 23);
 }
 
 __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const double* Cin,
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
       const bool in_range = eh >= 1023 - 200 && eh <= 1023 + 200;
       extreme |= h != 0.0 && !in_range;
       const float sv = in_range ? rsqrt_f32_of(h) : 0.0f;
-      for (int c = lane; c < i; c += 32) U32[e2::uoff(i) + c] = (float)row[c] * sv;
+      for (int c = lane; c < i; c += 32) U32[e2::uoff(i) + c] = d2f_bits(row[c]) * sv;
       if (lane == 0) Act32[i] = in_range ? 1.0f : 0.0f;
     } else {
       for (int c = lane; c < i; c += 32) U[e2::uoff(i) + c] = row[c];
@@ -273,7 +273,9 @@ __device__ inline LT make_rot(double c, double s);
 template <>
 __device__ inline double2 make_rot<double2>(double c, double s) { return make_double2(c, s); }
 template <>
-__device__ inline float2 make_rot<float2>(double c, double s) { return make_float2((float)c, (float)s); }
+__device__ inline float2 make_rot<float2>(double c, double s) {
+  return make_float2(d2f_bits(c), d2f_bits(s));  // not on the FP64 pipe
+}
 
 // LT: element type of the rotation log (double2 for the FP64 path, float2 when the
 // rotations are only replayed in FP32 by the mixed-precision vector kernel)
@@ -387,7 +389,7 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
     const double km1 = (double)(n - 1);
     for (int i = 0; i < n; ++i) {
       const double li = DD(i) * 1.0 + shift;
-      fl[i] = make_float2((float)(1.0 / li), (float)(sqrt(km1 / li) - srho));
+      fl[i] = make_float2(d2f_bits(1.0 / li), d2f_bits(sqrt(km1 / li) - srho));
     }
   } else {
     for (int i = 0; i < n; ++i) lam[(size_t)s * n + i] = DD(i) * 1.0 + shift;
@@ -411,6 +413,13 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
                                                   int rot_cap, const double* xb,
                                                   const double* axb, double* xa, double* axa) {
   constexpr bool kF32 = sizeof(VT) == sizeof(float);  // mixed path: FP32 reflectors and factors
+  // FP32 <-> FP64 conversions of the mixed path by bit operations (off the FP64 pipe)
+  auto to_vt = [](double x) -> VT {
+    if constexpr (kF32) return d2f_bits(x); else return x;
+  };
+  auto to_d = [](VT x) -> double {
+    if constexpr (kF32) return f2d_bits(x); else return x;
+  };
   const int n = g.ens;
   const bool vertical = g.vert_dist > 0.0;
   const int nvec_max = 1 + (vertical ? g.n_var : g.n);
@@ -457,10 +466,10 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
   if (work) {
     // load x
     if (v == 0) {
-      for (int i = 0; i < n; ++i) YY(i) = (VT)tin[(size_t)s * n + i];
+      for (int i = 0; i < n; ++i) YY(i) = to_vt(tin[(size_t)s * n + i]);
     } else {
       const double* xr = xb + (size_t)n * (r_state + (size_t)g.n * ci);
-      for (int i = 0; i < n; ++i) YY(i) = (VT)xr[i];
+      for (int i = 0; i < n; ++i) YY(i) = to_vt(xr[i]);
     }
     // y = Q^T x = P_1 ... P_{n-1} x  (P_{n-1} first)
     if constexpr (kF32) {
@@ -565,12 +574,13 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
     const double ab = axb[r_state + (size_t)g.n * ci];
     const double* xr = xb + (size_t)n * (r_state + (size_t)g.n * ci);
     double mean = 0.0;
+    const double dotw_d = to_d(dotw);
     for (int ee = 0; ee < n; ++ee)
-      mean += ab + (srho * xr[ee] + ((double)YY(ee) + (double)dotw));
+      mean += ab + (srho * xr[ee] + (to_d(YY(ee)) + dotw_d));
     mean /= (double)n;
     double* xo = xa + (size_t)n * (r_state + (size_t)g.n * ci);
     for (int ee = 0; ee < n; ++ee)
-      xo[ee] = (ab + (srho * xr[ee] + ((double)YY(ee) + (double)dotw))) - mean;
+      xo[ee] = (ab + (srho * xr[ee] + (to_d(YY(ee)) + dotw_d))) - mean;
     axa[r_state + (size_t)g.n * ci] = mean;
   }
 #undef YY

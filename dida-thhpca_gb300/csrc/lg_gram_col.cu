@@ -150,12 +150,14 @@ __device__ inline void level_window(const Geometry& g, const ListDev& l, const R
   const int glat = col % g.num_lat + 1, glon = col / g.num_lat + 1;
   const size_t ci = (size_t)(glat - 1 + g.halo) +
                     (size_t)(g.num_lat + 2 * g.halo) * (size_t)(glon - 1 + g.halo);
-  const double aps = axb[g.ps_row + (size_t)g.n * ci];
+  // in FP32 (the weights it feeds are FP32), converted without the FP64 pipe
+  const float aps = d2f_bits(axb[g.ps_row + (size_t)g.n * ci]);
+  const float ptop = d2f_bits(g.ptop), p0 = d2f_bits(g.p0);
   auto lev = [&](int k1) {
-    if (g.vcoord == LG_VCOORD_SIGMA) return g.ca[k1 - 1] * (aps - g.ptop) + g.ptop;
-    return g.ca[k1 - 1] * (g.p0 - g.ptop) + g.cb[k1 - 1] * (aps - g.ptop) + g.ptop;
+    if (g.vcoord == LG_VCOORD_SIGMA) return d2f_bits(g.ca[k1 - 1]) * (aps - ptop) + ptop;
+    return d2f_bits(g.ca[k1 - 1]) * (p0 - ptop) + d2f_bits(g.cb[k1 - 1]) * (aps - ptop) + ptop;
   };
-  al = (float)log(0.5 * (lev(kk) + lev(kk + 1)));
+  al = logf(0.5f * (lev(kk) + lev(kk + 1)));
   const float span = 2.0f * (float)g.vert_dist;
   int b_lo = (int)floorf((al - span - rec.lo) * rec.inv_dz) - 1;
   int b_hi = (int)floorf((al + span - rec.lo) * rec.inv_dz) + 1;
@@ -527,9 +529,9 @@ __global__ void __maxnreg__(128)
         conv_sync();
         for (int idx = tid; idx < k * k; idx += kConv) {
           const int i = idx % k, j = idx / k;
-          C[idx] = (double)(i >= j ? S[i * kDS + j] : S[j * kDS + i]);
+          C[idx] = f2d_bits(i >= j ? S[i * kDS + j] : S[j * kDS + i]);
         }
-        if (tid < k) t[tid] = (double)((s_t[0][tid] + s_t[1][tid]) + (s_t[2][tid] + s_t[3][tid]));
+        if (tid < k) t[tid] = f2d_bits((s_t[0][tid] + s_t[1][tid]) + (s_t[2][tid] + s_t[3][tid]));
         conv_sync();
       }
       tc::fence_before();

@@ -393,8 +393,11 @@ def main():
             t1 = time.perf_counter()
             ctx.letkf_run(0, nxb, naxb, nxa, naxa)
             ts.append(time.perf_counter() - t0)
-            print("e2e step: lg_set_obs %.1f ms, lg_run %.1f ms (device analysis %.1f ms)" % (
-                1e3 * (t1 - t0), 1e3 * (ts[-1] - (t1 - t0)), ctx.stats()["ms_total"]), file=sys.stderr)
+            st_e = ctx.stats()
+            print("e2e step: lg_set_obs %.1f ms, lg_run %.1f ms (copy in %.1f ms, device analysis "
+                  "%.1f ms, copy out %.1f ms)" % (1e3 * (t1 - t0), 1e3 * (ts[-1] - (t1 - t0)),
+                                                 st_e["ms_h2d"], st_e["ms_total"], st_e["ms_d2h"]),
+                  file=sys.stderr)
         o = w.obs
         h2d = nxb.nbytes + naxb.nbytes + sum(a.nbytes for a in (o.type, o.lat, o.lon, o.ph, o.yo, o.rinv))
         h = cfg.halo

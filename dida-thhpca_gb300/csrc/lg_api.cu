@@ -100,6 +100,7 @@ struct lg_ctx {
   // [4] selection start, [5] selection end
   cudaEvent_t ev[6] = {};
   cudaEvent_t ev_hx = nullptr;  // H(x) done (orders the records and Grams after it)
+  cudaEvent_t ev_io[4] = {};    // lg_run: around the copy in, around the copy out
   std::vector<cudaEvent_t> kev;  // per-launch events of the solve phase
   unsigned long long* d_work = nullptr;
   // sizes fixed for the current observation set, and the captured analysis
@@ -261,7 +262,8 @@ void release_streams(lg_ctx* c) {
       cudaStreamDestroy(*sp);
       *sp = nullptr;
     }
-  for (cudaEvent_t* ep : {&c->ev_fork, &c->ev_join, &c->ev_join3, &c->ev_join4})
+  for (cudaEvent_t* ep : {&c->ev_fork, &c->ev_join, &c->ev_join3, &c->ev_join4, &c->ev_io[0],
+                          &c->ev_io[1], &c->ev_io[2], &c->ev_io[3]})
     if (*ep) {
       cudaEventDestroy(*ep);
       *ep = nullptr;
@@ -390,7 +392,9 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
               cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
               cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) == cudaSuccess &&
               cudaEventCreateWithFlags(&c->ev_join3, cudaEventDisableTiming) == cudaSuccess &&
-              cudaEventCreateWithFlags(&c->ev_join4, cudaEventDisableTiming) == cudaSuccess;
+              cudaEventCreateWithFlags(&c->ev_join4, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreate(&c->ev_io[0]) == cudaSuccess && cudaEventCreate(&c->ev_io[1]) == cudaSuccess &&
+              cudaEventCreate(&c->ev_io[2]) == cudaSuccess && cudaEventCreate(&c->ev_io[3]) == cudaSuccess;
   for (auto& row : c->ev_phase)
     for (auto& e : row)
       made = made && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
@@ -1176,21 +1180,27 @@ int lg_run(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* x
     c->state_elems = cols * n * k;
   }
   cudaStream_t st = c->own_stream;
+  CK(cudaEventRecord(c->ev_io[0], st));
   CK(cudaMemcpyAsync(c->d_xb, xb, sizeof(double) * cols * n * k, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->d_axb, axb, sizeof(double) * cols * n, cudaMemcpyHostToDevice, st));
+  CK(cudaEventRecord(c->ev_io[1], st));
   int r = lg_run_device(c, ntimes, c->d_xb, c->d_axb, c->d_xa, c->d_axa, st);
   if (r != LG_OK) return r;
   // interior columns only: for each longitude the interior latitudes are contiguous
   const size_t h = g.halo;
   const size_t pitch_x = nlat_e * n * k * sizeof(double), pitch_a = nlat_e * n * sizeof(double);
   const size_t off_x = (h + h * nlat_e) * n * k, off_a = (h + h * nlat_e) * n;
+  CK(cudaEventRecord(c->ev_io[2], st));
   CK(cudaMemcpy2DAsync(xa + off_x, pitch_x, c->d_xa + off_x, pitch_x,
                        (size_t)g.num_lat * n * k * sizeof(double), g.num_lon,
                        cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpy2DAsync(axa + off_a, pitch_a, c->d_axa + off_a, pitch_a,
                        (size_t)g.num_lat * n * sizeof(double), g.num_lon,
                        cudaMemcpyDeviceToHost, st));
+  CK(cudaEventRecord(c->ev_io[3], st));
   CK(cudaStreamSynchronize(st));
+  c->stats.ms_h2d = elapsed_ms(c->ev_io[0], c->ev_io[1]);
+  c->stats.ms_d2h = elapsed_ms(c->ev_io[2], c->ev_io[3]);
   return LG_OK;
 }
 

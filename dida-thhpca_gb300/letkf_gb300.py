@@ -73,7 +73,7 @@ class LgStats(C.Structure):
         ("ms_total", C.c_double), ("ms_gram", C.c_double), ("ms_eig", C.c_double),
         ("n_launches", C.c_int64), ("n_gram_entries", C.c_int64),
         ("ms_tridiag", C.c_double), ("ms_ql", C.c_double), ("ms_vec", C.c_double),
-        ("n_chunks", C.c_int64),
+        ("n_chunks", C.c_int64), ("ms_h2d", C.c_double), ("ms_d2h", C.c_double),
     ]
 
     def as_dict(self):

@@ -141,6 +141,8 @@ typedef struct lg_stats {
   double ms_ql;             /* implicit QL kernels */
   double ms_vec;            /* vector transform + update kernels (incl. overflow fallback) */
   int64_t n_chunks;         /* solve chunks (launches of each solve-phase kernel) */
+  double ms_h2d, ms_d2h;    /* lg_run only: background copy in before the analysis and
+                               analysis copy out after it (device events); 0 otherwise */
 } lg_stats;
 
 typedef struct lg_ctx lg_ctx;

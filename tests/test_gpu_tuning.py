@@ -65,8 +65,10 @@ def test_fp64_analysis_is_bit_identical_under_every_setting(monkeypatch):
         xa = np.zeros_like(w.xb)
         axa = np.zeros_like(w.axb)
         ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+        st = ctx.stats()
+        assert st["ms_h2d"] > 0.0 and st["ms_d2h"] > 0.0  # host-array run: copies timed
         tl = ctx.timeline()
-        assert tl.shape == (ctx.stats()["n_chunks"], 7) and tl.shape[0] >= 1
+        assert tl.shape == (st["n_chunks"], 7) and tl.shape[0] >= 1
         eps = 1e-3  # event timestamps are ms floats
         for a, b in ((0, 1), (1, 2), (2, 3), (3, 4), (4, 5), (5, 6)):
             assert np.all(tl[:, b] >= tl[:, a] - eps), (kw, a, b, tl)

@@ -75,6 +75,8 @@ struct lg_ctx {
   int rot_cap = 0;
   // extra solve streams (tune.solve_streams 2..4) and their ordering events
   cudaStream_t side_stream = nullptr, third_stream = nullptr, fourth_stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // lg_run: host copies beside the analysis
+  cudaEvent_t ev_copy_in = nullptr, ev_copy_join = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join3 = nullptr, ev_join4 = nullptr;
   // [Gram, tridiagonalisation (or eigensolve), QL, vectors done][buffer set]
   cudaEvent_t ev_phase[4][4] = {};
@@ -108,7 +110,7 @@ struct lg_ctx {
   int chunk = 1;
   bool use_eig2 = false;
   cudaGraphExec_t graph_exec = nullptr;
-  const void* graph_key[5] = {};
+  const void* graph_key[9] = {};
   int64_t graph_launches = 0;
   bool graph_failed = false;
 };
@@ -257,13 +259,15 @@ double box_bound(float v) {
 }
 
 void release_streams(lg_ctx* c) {
-  for (cudaStream_t* sp : {&c->own_stream, &c->side_stream, &c->third_stream, &c->fourth_stream})
+  for (cudaStream_t* sp : {&c->own_stream, &c->side_stream, &c->third_stream, &c->fourth_stream,
+                           &c->copy_stream})
     if (*sp) {
       cudaStreamDestroy(*sp);
       *sp = nullptr;
     }
   for (cudaEvent_t* ep : {&c->ev_fork, &c->ev_join, &c->ev_join3, &c->ev_join4, &c->ev_io[0],
-                          &c->ev_io[1], &c->ev_io[2], &c->ev_io[3]})
+                          &c->ev_io[1], &c->ev_io[2], &c->ev_io[3], &c->ev_copy_in,
+                          &c->ev_copy_join})
     if (*ep) {
       cudaEventDestroy(*ep);
       *ep = nullptr;
@@ -279,7 +283,7 @@ void release_streams(lg_ctx* c) {
 void drop_graph(lg_ctx* c) {
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   c->graph_exec = nullptr;
-  c->graph_key[0] = c->graph_key[1] = c->graph_key[2] = c->graph_key[3] = c->graph_key[4] = nullptr;
+  for (auto& p : c->graph_key) p = nullptr;
 }
 
 void free_obs(lg_ctx* c) {
@@ -394,7 +398,10 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
               cudaEventCreateWithFlags(&c->ev_join3, cudaEventDisableTiming) == cudaSuccess &&
               cudaEventCreateWithFlags(&c->ev_join4, cudaEventDisableTiming) == cudaSuccess &&
               cudaEventCreate(&c->ev_io[0]) == cudaSuccess && cudaEventCreate(&c->ev_io[1]) == cudaSuccess &&
-              cudaEventCreate(&c->ev_io[2]) == cudaSuccess && cudaEventCreate(&c->ev_io[3]) == cudaSuccess;
+              cudaEventCreate(&c->ev_io[2]) == cudaSuccess && cudaEventCreate(&c->ev_io[3]) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&c->ev_copy_in, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&c->ev_copy_join, cudaEventDisableTiming) == cudaSuccess;
   for (auto& row : c->ev_phase)
     for (auto& e : row)
       made = made && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
@@ -876,9 +883,48 @@ int prepare_capacity(lg_ctx* c) {
   return LG_OK;
 }
 
+// Host arrays of lg_run whose copies are part of the captured analysis (all
+// four pinned): the background goes in on the copy stream beside the
+// selection, and each chunk's analysed columns come out as soon as its vector
+// update is done, beside the later chunks.
+struct HostIO {
+  const double *xb, *axb;
+  double *xa, *axa;
+};
+
+// Interior columns [c0, c1) of a [lon + 2 halo][lat + 2 halo][epc] array, device
+// to host: a partial first longitude row, the full rows as one 2-D copy, a
+// partial last row.
+cudaError_t copy_cols_d2h(const lg_config& g, double* dst, const double* src, size_t epc, int c0,
+                          int c1, cudaStream_t s) {
+  const int nl = g.num_lat, h = g.halo;
+  const size_t nlat_e = (size_t)nl + 2 * h, pitch = nlat_e * epc * sizeof(double);
+  auto off = [&](int lat, int lon) { return ((size_t)(h + lat) + nlat_e * (size_t)(h + lon)) * epc; };
+  int c = c0;
+  while (c < c1) {
+    const int lon = c / nl, lat = c % nl;
+    if (lat == 0 && c + nl <= c1) {  // full rows
+      const int rows = (c1 - c) / nl;
+      cudaError_t e = cudaMemcpy2DAsync(dst + off(0, lon), pitch, src + off(0, lon), pitch,
+                                        (size_t)nl * epc * sizeof(double), rows,
+                                        cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) return e;
+      c += rows * nl;
+    } else {
+      const int lat1 = std::min(nl, lat + (c1 - c));
+      cudaError_t e = cudaMemcpyAsync(dst + off(lat, lon), src + off(lat, lon),
+                                      (size_t)(lat1 - lat) * epc * sizeof(double),
+                                      cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) return e;
+      c += lat1 - lat;
+    }
+  }
+  return cudaSuccess;
+}
+
 // Every kernel of one analysis, on stream st; no host synchronisation.
 int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, double* axa,
-                     cudaStream_t st, int64_t* launches_out) {
+                     cudaStream_t st, int64_t* launches_out, const HostIO* io = nullptr) {
   const lg_config& g = c->cfg;
   const Geometry& geo = c->geo;
   const int ncol = g.num_lat * g.num_lon;
@@ -893,6 +939,19 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   // only observation positions; the records and Grams wait for H(x))
   CK(cudaEventRecord(c->ev_fork, st));
   CK(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
+  if (io) {
+    // the background in, on the copy stream; H(x) (and everything after it) waits
+    const size_t cols = (size_t)(g.num_lat + 2 * g.halo) * (g.num_lon + 2 * g.halo);
+    CK(cudaStreamWaitEvent(c->copy_stream, c->ev_fork, 0));
+    CK(record_event(c->ev_io[0], c->copy_stream));
+    CK(cudaMemcpyAsync((void*)xb, io->xb, sizeof(double) * cols * c->geo.n * k,
+                       cudaMemcpyHostToDevice, c->copy_stream));
+    CK(cudaMemcpyAsync((void*)axb, io->axb, sizeof(double) * cols * c->geo.n,
+                       cudaMemcpyHostToDevice, c->copy_stream));
+    CK(record_event(c->ev_io[1], c->copy_stream));
+    CK(cudaEventRecord(c->ev_copy_in, c->copy_stream));
+    CK(cudaStreamWaitEvent(c->side_stream, c->ev_copy_in, 0));
+  }
   lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, c->side_stream);
   launches += c->obs.n_copies > 0;
   CK(record_event(c->ev[1], c->side_stream));
@@ -1052,7 +1111,14 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
       launches += 1;
     }
     CK(record_event(kv[6], s_v));
-    if (nl >= 3) CK(cudaEventRecord(c->ev_phase[3][set], s_v));
+    if (nl >= 3 || io) CK(cudaEventRecord(c->ev_phase[3][set], s_v));
+    if (io) {
+      // this chunk's columns are final: out beside the later chunks
+      CK(cudaStreamWaitEvent(c->copy_stream, c->ev_phase[3][set], 0));
+      const int c0 = b.first_col, c1 = b.first_col + b.ncols;
+      CK(copy_cols_d2h(g, io->xa, xa, (size_t)c->geo.n * k, c0, c1, c->copy_stream));
+      CK(copy_cols_d2h(g, io->axa, axa, (size_t)c->geo.n, c0, c1, c->copy_stream));
+    }
     launches += 1;
   }
   if (nl >= 2) {
@@ -1068,6 +1134,13 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     }
   }
   CK(record_event(c->ev[3], st));
+  if (io) {
+    // the copies not hidden behind the analysis
+    CK(record_event(c->ev_io[2], st));
+    CK(cudaEventRecord(c->ev_copy_join, c->copy_stream));
+    CK(cudaStreamWaitEvent(st, c->ev_copy_join, 0));
+    CK(record_event(c->ev_io[3], st));
+  }
   CK(cudaGetLastError());
   *launches_out = launches;
   return LG_OK;
@@ -1075,12 +1148,11 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
 
 }  // namespace
 
-int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* xa,
-                  double* axa, void* stream_v) {
-  (void)ntimes;
-  if (!c || !xb || !axb || !xa || !axa) return LG_ERR_ARG;
-  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
-  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+namespace {
+// One analysis on device arrays; with io, the host copies of lg_run run inside
+// it (see HostIO).
+int run_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, double* axa,
+                 cudaStream_t st, const HostIO* io) {
   const lg_config& g = c->cfg;
   const int ncol = g.num_lat * g.num_lon;
   lg_stats& S = c->stats;
@@ -1091,7 +1163,8 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   // The whole analysis is captured once into a CUDA graph per (arrays, stream)
   // and replayed afterwards; LETKF_GB300_NO_GRAPH=1 runs it eagerly.
   const bool graphs = !getenv("LETKF_GB300_NO_GRAPH") && !c->graph_failed;
-  const void* key[5] = {xb, axb, xa, axa, st};
+  const void* key[9] = {xb, axb, xa, axa, st, io ? io->xb : nullptr, io ? io->axb : nullptr,
+                        io ? io->xa : nullptr, io ? io->axa : nullptr};
   bool ran = false;
   if (graphs) {
     if (c->graph_exec && memcmp(key, c->graph_key, sizeof key) != 0) drop_graph(c);
@@ -1099,7 +1172,7 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
       cudaGraph_t graph = nullptr;
       bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess;
       int er = LG_OK;
-      if (ok) er = enqueue_analysis(c, xb, axb, xa, axa, st, &launches);
+      if (ok) er = enqueue_analysis(c, xb, axb, xa, axa, st, &launches, io);
       const cudaError_t ee = ok ? cudaStreamEndCapture(st, &graph) : cudaErrorUnknown;
       ok = ok && er == LG_OK && ee == cudaSuccess && graph != nullptr;
       if (ok)
@@ -1122,7 +1195,7 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
     }
   }
   if (!ran) {
-    r = enqueue_analysis(c, xb, axb, xa, axa, st, &launches);
+    r = enqueue_analysis(c, xb, axb, xa, axa, st, &launches, io);
     if (r != LG_OK) return r;
   }
   int status[4];
@@ -1158,8 +1231,31 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   S.nobsl_total = c->list_total;
   S.n_band = (int64_t)band;
   S.n_eig_fail = status[1];
+  if (io) {
+    S.ms_h2d = elapsed_ms(c->ev_io[0], c->ev_io[1]);
+    S.ms_d2h = elapsed_ms(c->ev_io[2], c->ev_io[3]);
+  }
   if (status[0] != 0) return status[0];
   return LG_OK;
+}
+
+bool pinned(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+}  // namespace
+
+int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* xa,
+                  double* axa, void* stream_v) {
+  (void)ntimes;
+  if (!c || !xb || !axb || !xa || !axa) return LG_ERR_ARG;
+  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
+  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+  return run_analysis(c, xb, axb, xa, axa, st, nullptr);
 }
 
 int lg_run(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* xa, double* axa) {
@@ -1180,6 +1276,11 @@ int lg_run(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* x
     c->state_elems = cols * n * k;
   }
   cudaStream_t st = c->own_stream;
+  if (pinned(xb) && pinned(axb) && pinned(xa) && pinned(axa)) {
+    // page-locked host arrays: the copies run inside the analysis, overlapped
+    const HostIO io{xb, axb, xa, axa};
+    return run_analysis(c, c->d_xb, c->d_axb, c->d_xa, c->d_axa, st, &io);
+  }
   CK(cudaEventRecord(c->ev_io[0], st));
   CK(cudaMemcpyAsync(c->d_xb, xb, sizeof(double) * cols * n * k, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->d_axb, axb, sizeof(double) * cols * n, cudaMemcpyHostToDevice, st));

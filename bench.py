@@ -385,6 +385,12 @@ def main():
         nxb, naxb, nxa, naxa = (t.numpy() for t in (hxb, haxb, hxa, haxa))
         ctx.set_obs(w.obs)
         ctx.letkf_run(0, nxb, naxb, nxa, naxa)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xb.copy_(hxb, non_blocking=True)
+        torch.cuda.synchronize()
+        print("e2e host buffers: pinned H2D %.1f GB/s" % (hxb.numel() * 8 / (time.perf_counter() - t0) / 1e9),
+              file=sys.stderr)
         ts = []
         for _ in range(args.e2e_steps):
             torch.cuda.synchronize()

@@ -123,6 +123,9 @@ class Config:
     n_clusters: int = 8
     cluster_sigma_deg: float = 5.0
     seed: int = 0
+    cube_n: int = 1      # da_block_interval: one solve per cube_n x cube_n columns
+    cube_nz: int = 1     # da_vertical_interval: one solve per cube_nz levels (vertical)
+    overlap: int = 0     # da_block_overlap: cubes step by cube_n - overlap, averaged
 
     @property
     def var_lev(self):
@@ -152,9 +155,9 @@ class Config:
         c.max_obs = self.max_obs
         c.global_nx = self.global_nx
         c.global_ny = self.global_ny
-        c.cube_n = 1
-        c.cube_nz = 1
-        c.overlap = 0
+        c.cube_n = self.cube_n
+        c.cube_nz = self.cube_nz
+        c.overlap = self.overlap
         c.precision = self.precision
         c.vcoord = self.vcoord
         return c

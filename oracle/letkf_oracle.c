@@ -832,17 +832,15 @@ static void ws_ensure(col_ws* w, int k, int nz, int need) {
   (void)nz;
 }
 
-static int analyse_column(const or_ctx* c, int col, const double* xb, const double* axb,
-                          double* xa, double* axa, col_ws* w, lg_stats* st) {
+/* gen_yb_dis[_vertical] for column col into w: yb, dep, rdiaginv, horizontal
+ * rloc and obs ln p of the list; returns nobsl (< 0 on a capacity error) */
+static int gather_list(const or_ctx* c, int col, col_ws* w, int* capped, int64_t* band) {
   const lg_config* g = &c->cfg;
-  const int k = g->ens, nz = g->nz, n = c->n;
-  const int glat = col % g->num_lat + 1, glon = col / g->num_lat + 1;
-  int capped = 0;
-  int64_t band = 0;
+  const int k = g->ens, nz = g->nz;
   int nobsl = or_column_list(c, col, NULL, NULL, 0, NULL, NULL);
   ws_ensure(w, k, nz, nobsl + 1);
-  nobsl = or_column_list(c, col, w->ent, w->rloc_h, w->cap, &capped, &band);
-  if (nobsl < 0) return LG_ERR_SHAPE;
+  nobsl = or_column_list(c, col, w->ent, w->rloc_h, w->cap, capped, band);
+  if (nobsl < 0) return nobsl;
   for (int i = 0; i < nobsl; ++i) {
     const int64_t ent = w->ent[i];
     memcpy(w->yb + (size_t)i * k, c->yb + (size_t)ent * k, sizeof(double) * k);
@@ -858,6 +856,18 @@ static int analyse_column(const or_ctx* c, int col, const double* xb, const doub
     w->rdiag[i] = (float)c->orinv[c->val_off[o] + m];
     w->lnp[i] = c->lnp[ent];
   }
+  return nobsl;
+}
+
+static int analyse_column(const or_ctx* c, int col, const double* xb, const double* axb,
+                          double* xa, double* axa, col_ws* w, lg_stats* st) {
+  const lg_config* g = &c->cfg;
+  const int k = g->ens, nz = g->nz, n = c->n;
+  const int glat = col % g->num_lat + 1, glon = col / g->num_lat + 1;
+  int capped = 0;
+  int64_t band = 0;
+  const int nobsl = gather_list(c, col, w, &capped, &band);
+  if (nobsl < 0) return LG_ERR_SHAPE;
   const size_t cc = col_index(g, glat, glon);
   double* xcol = xa + (size_t)k * n * cc;
   double* acol = axa + (size_t)n * cc;
@@ -927,12 +937,201 @@ static int analyse_column(const or_ctx* c, int col, const double* xb, const doub
   return LG_OK;
 }
 
-/* analysis of global columns [c0, c1) after or_hx */
+/* One cube of letkf_compute_nooverlap[_vertical] (letkf_compute.F90:12-154,
+ * 386-554) or of letkf_compute with overlapping cubes (:156-256): block b,
+ * block-local latitudes sj..ej and longitudes si..ei (1-based).  The list is
+ * the one of the cube's centre grid point (gen_yb_dis at grid((sj+ej)/2),
+ * grid((si+ei)/2), letkf_yb.F90:23-24,165-166).
+ *   accumulate = 0: xb_2_xa / the vertical update into xa, then recentred;
+ *   accumulate = 1: xb_add2_xa (:332-382): each column's recentred analysis
+ *                   and mean are added to xa, axa (averaged by the caller). */
+static int analyse_cube(const or_ctx* c, int b, int sj, int ej, int si, int ei, const double* xb,
+                        const double* axb, double* xa, double* axa, col_ws* w, lg_stats* st,
+                        int accumulate) {
+  const lg_config* g = &c->cfg;
+  const int k = g->ens, nz = g->nz, n = c->n;
+  const int glat0 = c->bs_lat[b] - 1, glon0 = c->bs_lon[b] - 1;  /* local 1 -> global */
+  const int cglat = glat0 + (sj + ej) / 2, cglon = glon0 + (si + ei) / 2;
+  const int ccol = (cglon - 1) * g->num_lat + (cglat - 1);
+  int capped = 0;
+  int64_t band = 0;
+  const int nobsl = gather_list(c, ccol, w, &capped, &band);
+  if (nobsl < 0) return LG_ERR_SHAPE;
+  int ierr = 0;
+  if (accumulate || g->vert_dist <= 0.0) {
+    ierr |= core_ws(k, nobsl, w->yb, w->rdiag, w->dep, w->rloc_h, g->inflation, w->trans, w->wbar,
+                    w->ws, w->iws);
+    if (st) st->n_solves++;
+    for (int ii = si; ii <= ei; ++ii)
+      for (int jj = sj; jj <= ej; ++jj) {
+        const size_t cc = col_index(g, glat0 + jj, glon0 + ii);
+        double* xcol = xa + (size_t)k * n * cc;
+        double* acol = axa + (size_t)n * cc;
+        const double* xbc = xb + (size_t)k * n * cc;
+        const double* abc = axb + (size_t)n * cc;
+        for (int r = 0; r < n; ++r) {
+          double* dist = w->xcol;  /* k */
+          double mean = 0.0;
+          for (int e = 0; e < k; ++e) {
+            double sum = 0.0;
+            for (int i = 0; i < k; ++i) sum += xbc[i + (size_t)k * r] * w->trans[i + k * e];
+            dist[e] = abc[r] + sum;
+            mean = mean + dist[e];
+          }
+          mean = mean / (double)k;
+          if (accumulate) {
+            acol[r] += mean;
+            for (int e = 0; e < k; ++e) xcol[e + (size_t)k * r] += dist[e] - mean;
+          } else {
+            acol[r] = mean;
+            for (int e = 0; e < k; ++e) xcol[e + (size_t)k * r] = dist[e] - mean;
+          }
+        }
+      }
+  } else {
+    /* ps2alnp at the centre column, one solve per level group */
+    const double aps = axb[(size_t)n * col_index(g, cglat, cglon) + g->ps_index - 1];
+    for (int i = 1; i <= nz; ++i) {
+      double v = 0.5 * (calc_ph_lev(c, i, aps) + calc_ph_lev(c, i + 1, aps));
+      w->alnp[i - 1] = log(v);
+    }
+    for (int kk = 1; kk <= nz; kk += g->cube_nz) {
+      const int sk = kk, ek = kk + g->cube_nz - 1 > nz ? nz : kk + g->cube_nz - 1;
+      const double al = w->alnp[(sk + ek) / 2 - 1];
+      for (int i = 0; i < nobsl; ++i) {  /* vertical_localization (letkf_yb.F90:240-260) */
+        double z = fabs(al - w->lnp[i]) / g->vert_dist;
+        w->rloc[i] = w->rloc_h[i] * (g->gc_filter_vertical ? or_schr2(z) : or_schr(z));
+      }
+      ierr |= core_ws(k, nobsl, w->yb, w->rdiag, w->dep, w->rloc, g->inflation, w->trans, w->wbar,
+                      w->ws, w->iws);
+      if (st) st->n_solves++;
+      for (int ii = si; ii <= ei; ++ii)
+        for (int jj = sj; jj <= ej; ++jj) {
+          const size_t cc = col_index(g, glat0 + jj, glon0 + ii);
+          double* xcol = xa + (size_t)k * n * cc;
+          const double* xbc = xb + (size_t)k * n * cc;
+          const double* abc = axb + (size_t)n * cc;
+          for (int v = 0; v < g->n_var; ++v) {
+            int r0, r1;  /* 0-based rows updated by this group */
+            if (g->var_lev[v] == 1) {
+              if (ek != nz) continue;
+              r0 = r1 = c->var_start[v] - 1;
+            } else {
+              r0 = c->var_start[v] + sk - 2;
+              r1 = c->var_start[v] + ek - 2;
+            }
+            for (int r = r0; r <= r1; ++r)
+              for (int e = 0; e < k; ++e) {
+                double sum = 0.0;
+                for (int i = 0; i < k; ++i) sum += xbc[i + (size_t)k * r] * w->trans[i + k * e];
+                xcol[e + (size_t)k * r] = abc[r] + sum;
+              }
+          }
+        }
+    }
+    /* recentre the cube's columns (letkf_compute.F90:539-552) */
+    for (int ii = si; ii <= ei; ++ii)
+      for (int jj = sj; jj <= ej; ++jj) {
+        const size_t cc = col_index(g, glat0 + jj, glon0 + ii);
+        double* xcol = xa + (size_t)k * n * cc;
+        double* acol = axa + (size_t)n * cc;
+        for (int r = 0; r < n; ++r) {
+          double sum = 0.0;
+          for (int e = 0; e < k; ++e) sum = sum + xcol[e + (size_t)k * r];
+          sum = sum / (double)k;
+          acol[r] = sum;
+          for (int e = 0; e < k; ++e) xcol[e + (size_t)k * r] = xcol[e + (size_t)k * r] - sum;
+        }
+      }
+  }
+  if (st) {
+    st->n_columns += (int64_t)(ei - si + 1) * (ej - sj + 1);
+    st->nobsl_total += nobsl;
+    if (nobsl > st->nobsl_max) st->nobsl_max = nobsl;
+    st->n_capped += capped;
+    st->n_band += band;
+    st->n_eig_fail += ierr != 0;
+  }
+  return LG_OK;
+}
+
+/* cube analysis of block b: the cube loops of letkf_compute_nooverlap[_vertical]
+ * (overlap 0: stride cube_n) or letkf_compute (stride cube_n - overlap, each
+ * column averaged over the cubes that cover it) */
+static int analyse_block_cubes(const or_ctx* c, int b, const double* xb, const double* axb,
+                               double* xa, double* axa, col_ws* w, lg_stats* st) {
+  const lg_config* g = &c->cfg;
+  const int k = g->ens, n = c->n;
+  const int nxl = c->be_lat[b] - c->bs_lat[b] + 1, nyl = c->be_lon[b] - c->bs_lon[b] + 1;
+  const int ov = g->overlap, stride = g->cube_n - ov;
+  int status = LG_OK;
+  double* cnt = NULL;
+  if (ov > 0) {
+    cnt = (double*)calloc((size_t)nxl * nyl, sizeof(double));
+    for (int ii = 1; ii <= nyl; ++ii)
+      for (int jj = 1; jj <= nxl; ++jj) {
+        const size_t cc = col_index(g, c->bs_lat[b] - 1 + jj, c->bs_lon[b] - 1 + ii);
+        memset(xa + (size_t)k * n * cc, 0, sizeof(double) * k * n);
+        memset(axa + (size_t)n * cc, 0, sizeof(double) * n);
+      }
+  }
+  for (int i = 1; i <= nyl; i += stride) {
+    const int si = i, ei = i + g->cube_n - 1 > nyl ? nyl : i + g->cube_n - 1;
+    for (int j = 1; j <= nxl; j += stride) {
+      const int sj = j, ej = j + g->cube_n - 1 > nxl ? nxl : j + g->cube_n - 1;
+      const int r = analyse_cube(c, b, sj, ej, si, ei, xb, axb, xa, axa, w, st, ov > 0);
+      if (r != LG_OK) status = r;
+      if (cnt)
+        for (int ii = si; ii <= ei; ++ii)
+          for (int jj = sj; jj <= ej; ++jj) cnt[(size_t)(ii - 1) * nxl + (jj - 1)] += 1.0;
+    }
+  }
+  if (cnt) {
+    for (int ii = 1; ii <= nyl; ++ii)
+      for (int jj = 1; jj <= nxl; ++jj) {
+        const double q = cnt[(size_t)(ii - 1) * nxl + (jj - 1)];
+        const size_t cc = col_index(g, c->bs_lat[b] - 1 + jj, c->bs_lon[b] - 1 + ii);
+        for (size_t e = 0; e < (size_t)k * n; ++e) xa[(size_t)k * n * cc + e] /= q;
+        for (int r = 0; r < n; ++r) axa[(size_t)n * cc + r] /= q;
+      }
+    free(cnt);
+  }
+  return status;
+}
+
+/* letkf_core on column col's horizontal list (gen_yb_dis + letkf_core):
+ * trans(k x k, column-major), for tests of the cube paths */
+int or_column_trans(const or_ctx* c, int col, double* trans) {
+  if (!c->hx_done) return LG_ERR_STATE;
+  const int k = c->cfg.ens;
+  col_ws w;
+  memset(&w, 0, sizeof w);
+  w.iws = (int*)malloc(sizeof(int) * (5 * k + 3));
+  w.wbar = (double*)malloc(sizeof(double) * k);
+  int capped = 0;
+  int64_t band = 0;
+  const int nobsl = gather_list(c, col, &w, &capped, &band);
+  int r = nobsl < 0 ? LG_ERR_SHAPE : LG_OK;
+  if (r == LG_OK && core_ws(k, nobsl, w.yb, w.rdiag, w.dep, w.rloc_h, c->cfg.inflation, trans,
+                            w.wbar, w.ws, w.iws) != 0)
+    r = LG_ERR_EIG;
+  free(w.ent); free(w.rloc_h); free(w.rloc); free(w.rdiag); free(w.dep); free(w.yb); free(w.lnp);
+  free(w.ws); free(w.iws); free(w.wbar);
+  return r;
+}
+
+/* analysis of global columns [c0, c1) after or_hx; with cubes, the whole globe */
 int or_analysis(const or_ctx* c, const double* xb, const double* axb, double* xa, double* axa,
                 int c0, int c1, int nthreads, lg_stats* st_out) {
   if (!c->hx_done) return LG_ERR_STATE;
   const lg_config* g = &c->cfg;
   const int k = g->ens;
+  /* cube_n > 1, cube_nz > 1 or overlap > 0: whole blocks of cubes (the whole
+   * globe only; overlapping cubes are averaged across each block) */
+  const int cubes = g->cube_n > 1 || g->overlap > 0 || (g->cube_nz > 1 && g->vert_dist > 0.0);
+  if (g->cube_n < 1 || g->cube_nz < 1 || g->overlap < 0 || g->overlap >= g->cube_n)
+    return LG_ERR_ARG;  /* the reference's cube loops would not advance */
+  if (cubes && (c0 != 0 || c1 != g->num_lat * g->num_lon)) return LG_ERR_ARG;
   int status = LG_OK;
   lg_stats tot;
   memset(&tot, 0, sizeof tot);
@@ -947,14 +1146,26 @@ int or_analysis(const or_ctx* c, const double* xb, const double* axb, double* xa
     w.trans = (double*)malloc(sizeof(double) * k * k);
     w.wbar = (double*)malloc(sizeof(double) * k);
     w.alnp = (double*)malloc(sizeof(double) * (g->nz + 1));
+    w.xcol = (double*)malloc(sizeof(double) * k);
     lg_stats st;
     memset(&st, 0, sizeof st);
+    if (cubes) {
+      /* cubes never cross blocks: blocks in parallel, each block's cubes in order */
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 1)
 #endif
-    for (int col = c0; col < c1; ++col) {
-      int s = analyse_column(c, col, xb, axb, xa, axa, &w, &st);
-      if (s != LG_OK) status = s;
+      for (int b = 0; b < c->nblocks; ++b) {
+        int s = analyse_block_cubes(c, b, xb, axb, xa, axa, &w, &st);
+        if (s != LG_OK) status = s;
+      }
+    } else {
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+      for (int col = c0; col < c1; ++col) {
+        int s = analyse_column(c, col, xb, axb, xa, axa, &w, &st);
+        if (s != LG_OK) status = s;
+      }
     }
 #ifdef _OPENMP
 #pragma omp critical
@@ -969,7 +1180,7 @@ int or_analysis(const or_ctx* c, const double* xb, const double* axb, double* xa
       tot.n_eig_fail += st.n_eig_fail;
     }
     free(w.ent); free(w.rloc_h); free(w.rloc); free(w.rdiag); free(w.dep); free(w.yb); free(w.lnp);
-    free(w.ws); free(w.iws); free(w.trans); free(w.wbar); free(w.alnp);
+    free(w.ws); free(w.iws); free(w.trans); free(w.wbar); free(w.alnp); free(w.xcol);
   }
   tot.n_copies = c->n_copies;
   tot.n_entries = c->n_entries;

@@ -57,6 +57,7 @@ def lib(use_lapack: bool = True):
                                  P(C.c_int), P(C.c_int64)]
     L.or_analysis.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), P(C.c_double),
                               P(C.c_double), C.c_int, C.c_int, C.c_int, P(LgStats)]
+    L.or_column_trans.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
     L.or_core.argtypes = [C.c_int, C.c_int, P(C.c_double), P(C.c_float), P(C.c_double),
                           P(C.c_double), C.c_double, P(C.c_double), P(C.c_double)]
     L.or_latlon_dist_r8.restype = C.c_double
@@ -148,6 +149,16 @@ class Oracle:
                                   C.byref(capped), C.byref(band))
         assert n2 == n
         return ent[:n], rl[:n]
+
+    def column_trans(self, col: int):
+        """letkf_core on column col's horizontal list: trans[j, i] = Fortran
+        trans(i, j) (the k x k array, column-major in memory)."""
+        k = self.cfg.ens
+        t = np.zeros((k, k))
+        r = lib().or_column_trans(self.h, col, _p(t, C.c_double))
+        if r != 0:
+            raise RuntimeError(f"or_column_trans: {r}")
+        return t
 
     def analysis(self, xb, axb, xa, axa, c0=0, c1=None, nthreads: int = 0):
         if c1 is None:

@@ -189,3 +189,122 @@ def test_post_processing_kat():
             assert np.allclose(xo[1:-1, j + 1], (axb[..., None] + xb)[1:-1, j + 1])
     assert np.allclose(sb[:, :, 0], np.sqrt((xb[1:-1, 1:-1, 0] ** 2).mean(-1)))
     assert (xo[0] == 0).all()
+
+
+def _block_bounds(n, nb):
+    """pro_info_get_indx (pro_info.F90:96-125): 1-based (start, end) per block."""
+    sec, res = n // nb, n % nb
+    out = []
+    for b in range(1, nb + 1):
+        if b - 1 < res:
+            s = (b - 1) * (sec + 1) + 1
+            out.append((s, s + sec))
+        else:
+            s = (b - 1) * sec + res + 1
+            out.append((s, s + sec - 1))
+    return out
+
+
+def _cube_expected(cfg, w, o):
+    """The cube loops of letkf_compute_nooverlap (overlap 0) and letkf_compute
+    (overlap > 0, letkf_compute.F90:12-154, 156-256) restated in numpy for a
+    horizontal-only configuration, each cube's trans from its centre column."""
+    h, k = cfg.halo, cfg.ens
+    xb, axb = w.xb, w.axb
+    xa = np.zeros_like(xb)
+    axa = np.zeros_like(axb)
+    cnt = np.zeros(axb.shape[:2])
+    ncubes = 0
+    stride = cfg.cube_n - cfg.overlap
+    for (la0, la1) in _block_bounds(cfg.num_lat, cfg.global_nx):
+        for (lo0, lo1) in _block_bounds(cfg.num_lon, cfg.global_ny):
+            nxl, nyl = la1 - la0 + 1, lo1 - lo0 + 1
+            for i in range(1, nyl + 1, stride):
+                si, ei = i, min(i + cfg.cube_n - 1, nyl)
+                for j in range(1, nxl + 1, stride):
+                    sj, ej = j, min(j + cfg.cube_n - 1, nxl)
+                    cglat, cglon = la0 - 1 + (sj + ej) // 2, lo0 - 1 + (si + ei) // 2
+                    t = o.column_trans((cglon - 1) * cfg.num_lat + (cglat - 1))
+                    ncubes += 1
+                    for ii in range(si, ei + 1):
+                        for jj in range(sj, ej + 1):
+                            x, y = h + lo0 - 1 + ii - 1, h + la0 - 1 + jj - 1
+                            dist = axb[x, y][:, None] + xb[x, y] @ t.T
+                            mean = dist.mean(axis=1)
+                            xa[x, y] += dist - mean[:, None]
+                            axa[x, y] += mean
+                            cnt[x, y] += 1
+    inner = (slice(h, -h), slice(h, -h))
+    assert np.all(cnt[inner] >= 1)
+    xa[inner] /= cnt[inner][..., None, None]
+    axa[inner] /= cnt[inner][..., None]
+    return xa, axa, ncubes
+
+
+@pytest.mark.parametrize("cube_n,overlap", [(3, 0), (3, 1), (2, 1)])
+def test_cube_analysis_matches_numpy_restatement(cube_n, overlap):
+    """Horizontal cubes (one solve per cube from its centre column's list),
+    with and without overlap (averaged over the covering cubes)."""
+    import letkf_gb300 as lg
+    import synth
+    from oracle import oracle as orc
+    cfg = lg.preset("tiny2d").replace(cube_n=cube_n, overlap=overlap)
+    w = synth.make_workload(cfg)
+    o = orc.Oracle(cfg, w.obs)
+    o.hx(w.xb, w.axb)
+    xa = np.zeros_like(w.xb)
+    axa = np.zeros_like(w.axb)
+    st = o.analysis(w.xb, w.axb, xa, axa)
+    xe, ae, ncubes = _cube_expected(cfg, w, o)
+    h = cfg.halo
+    full = (xa + axa[..., None])[h:-h, h:-h]
+    full_e = (xe + ae[..., None])[h:-h, h:-h]
+    scale = np.abs(full_e).max()
+    assert np.abs(full - full_e).max() <= 1e-12 * scale
+    assert st["n_solves"] == ncubes and st["n_columns"] >= cfg.num_lat * cfg.num_lon
+
+
+def test_cube_centre_columns_and_levels_match_per_column_analysis():
+    """Vertical path: with cube_n = 2 the centre column of every cube has the
+    per-column analysis; with cube_nz = 3 the 3-D rows at each level group's
+    centre level have it (the group's solve is the centre level's)."""
+    import letkf_gb300 as lg
+    import synth
+    from oracle import oracle as orc
+    base = lg.preset("tiny3d")
+    w = synth.make_workload(base)
+
+    def run(cfg):
+        o = orc.Oracle(cfg, w.obs)
+        o.hx(w.xb, w.axb)
+        xa = np.zeros_like(w.xb)
+        axa = np.zeros_like(w.axb)
+        o.analysis(w.xb, w.axb, xa, axa)
+        return xa, axa
+
+    ref = run(base)
+    h = base.halo
+    cub = run(base.replace(cube_n=2))
+    for (la0, la1) in _block_bounds(base.num_lat, base.global_nx):
+        for (lo0, lo1) in _block_bounds(base.num_lon, base.global_ny):
+            nxl, nyl = la1 - la0 + 1, lo1 - lo0 + 1
+            for i in range(1, nyl + 1, 2):
+                ci = (i + min(i + 1, nyl)) // 2
+                for j in range(1, nxl + 1, 2):
+                    cj = (j + min(j + 1, nxl)) // 2
+                    x, y = h + lo0 - 1 + ci - 1, h + la0 - 1 + cj - 1
+                    assert np.array_equal(cub[0][x, y], ref[0][x, y])
+                    assert np.array_equal(cub[1][x, y], ref[1][x, y])
+    vz = run(base.replace(cube_nz=3))
+    rows = []
+    r0 = 0
+    for name, lv in zip(base.var_names, base.var_lev):
+        if lv > 1:
+            for sk in range(1, base.nz + 1, 3):
+                ek = min(sk + 2, base.nz)
+                rows.append(r0 + (sk + ek) // 2 - 1)
+        r0 += lv
+    inner = (slice(h, -h), slice(h, -h))
+    assert np.array_equal(vz[0][inner][:, :, rows], ref[0][inner][:, :, rows])
+    other = [r for r in range(base.n_rows) if r not in rows]
+    assert not np.array_equal(vz[0][inner][:, :, other], ref[0][inner][:, :, other])

@@ -108,6 +108,14 @@ struct lg_ctx {
   // sizes fixed for the current observation set, and the captured analysis
   bool capacity_ready = false;
   int chunk = 1;
+  // cube solves (cube_n > 1, cube_nz > 1 on the vertical path, or overlap > 0)
+  bool cubes = false;
+  bool cube_plan = false;
+  int cube_ns = 0, cube_cs = 1, cube_ngroups = 1;  // solves, solves per chunk, level groups
+  int* d_cube_off = nullptr;
+  int *d_s_col = nullptr, *d_s_kk = nullptr;
+  double* d_trans = nullptr;
+  size_t trans_cap = 0;
   bool use_eig2 = false;
   cudaGraphExec_t graph_exec = nullptr;
   const void* graph_key[9] = {};
@@ -359,7 +367,8 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
       g.global_nx > g.num_lat || g.global_ny > g.num_lon || g.local_dist <= 0.0 ||
       g.inflation <= 0.0 || g.ps_index < 1)
     return LG_ERR_ARG;
-  if (g.cube_n != 1 || g.cube_nz != 1 || g.overlap != 0) return LG_ERR_UNSUPPORTED;
+  // cubes (letkf_compute.F90): the loops step by cube_n - overlap
+  if (g.cube_n < 1 || g.cube_nz < 1 || g.overlap < 0 || g.overlap >= g.cube_n) return LG_ERR_ARG;
   if (g.precision != LG_PREC_FP64 && g.precision != LG_PREC_MIXED) return LG_ERR_ARG;
   int rows = 0;
   for (int v = 0; v < g.n_var; ++v) {
@@ -369,6 +378,10 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   if (g.ps_index > rows) return LG_ERR_ARG;
   lg_ctx* c = new lg_ctx();
   c->cfg = g;
+  // overlapping cubes: letkf_run takes letkf_compute, which has no vertical
+  // localisation, whatever da_vert_distance is (letkf.F90:227-235)
+  if (g.overlap > 0) c->cfg.vert_dist = 0.0;
+  c->cubes = g.cube_n > 1 || g.overlap > 0 || (g.cube_nz > 1 && c->cfg.vert_dist > 0.0);
   cudaGetDevice(&c->dev);
   // Scheduling priorities of the solve streams (Gram, vector update, QL): a
   // level 0 (lowest, the default stream's), 1 or 2 (highest) each.  Pending
@@ -430,7 +443,7 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   geo.ps_row = g.ps_index - 1;
   geo.vcoord = g.vcoord;
   geo.local_dist = g.local_dist;
-  geo.vert_dist = g.vert_dist;
+  geo.vert_dist = c->cfg.vert_dist;  // 0 with overlapping cubes (see above)
   geo.inflation = g.inflation;
   geo.obs_polar = g.obs_polar;
   geo.gc_filter = g.gc_filter;
@@ -785,6 +798,52 @@ float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
 // so their total is known before any background arrives.  After this, an
 // analysis enqueues work only (no host synchronisation, no allocation), which
 // lets lg_run_device capture it into a CUDA graph.
+// Cubes of each block (cube_n x cube_n columns stepping by cube_n - overlap,
+// clipped at the block edge, letkf_compute.F90:52-66, 176-192) and their level
+// groups (cube_nz levels on the vertical path, :431-436): the centre column
+// ((sj + ej) / 2, (si + ei) / 2) and centre level ((sk + ek) / 2) of every solve.
+// Fixed by the grid and configuration, so built once per context.
+int build_cube_plan(lg_ctx* c) {
+  if (c->cube_plan) return LG_OK;
+  const lg_config& g = c->cfg;
+  const int nb = g.global_nx * g.global_ny;
+  const int cn = g.cube_n, st = g.cube_n - g.overlap;
+  const bool grouped = g.vert_dist > 0.0 && g.overlap == 0;
+  const int ng = grouped ? (g.nz + g.cube_nz - 1) / g.cube_nz : 1;
+  std::vector<int> off(nb + 1, 0), s_col, s_kk;
+  for (int b = 0; b < nb; ++b) {
+    const int4 bk = c->blk[b];
+    const int nxl = bk.y - bk.x + 1, nyl = bk.w - bk.z + 1;
+    const int ncj = (nxl - 1) / st + 1, nci = (nyl - 1) / st + 1;
+    off[b + 1] = off[b] + ncj * nci;
+    for (int mi = 0; mi < nci; ++mi) {
+      const int si = 1 + mi * st, ei = std::min(si + cn - 1, nyl);
+      for (int mj = 0; mj < ncj; ++mj) {
+        const int sj = 1 + mj * st, ej = std::min(sj + cn - 1, nxl);
+        const int glat = bk.x - 1 + (sj + ej) / 2, glon = bk.z - 1 + (si + ei) / 2;
+        const int col = (glon - 1) * g.num_lat + (glat - 1);
+        for (int gi = 0; gi < ng; ++gi) {
+          const int sk = gi * g.cube_nz + 1, ek = std::min(sk + g.cube_nz - 1, g.nz);
+          s_col.push_back(col);
+          s_kk.push_back(grouped ? (sk + ek) / 2 : 1);
+        }
+      }
+    }
+  }
+  int r = LG_OK;
+  r |= dalloc(&c->d_cube_off, off.size());
+  r |= dalloc(&c->d_s_col, s_col.size());
+  r |= dalloc(&c->d_s_kk, s_kk.size());
+  if (r != LG_OK) return LG_ERR_NOMEM;
+  CK(cudaMemcpy(c->d_cube_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_s_col, s_col.data(), sizeof(int) * s_col.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_s_kk, s_kk.data(), sizeof(int) * s_kk.size(), cudaMemcpyHostToDevice));
+  c->cube_ns = (int)s_col.size();
+  c->cube_ngroups = ng;
+  c->cube_plan = true;
+  return LG_OK;
+}
+
 int prepare_capacity(lg_ctx* c) {
   if (c->capacity_ready) return LG_OK;
   const lg_config& g = c->cfg;
@@ -843,6 +902,38 @@ int prepare_capacity(lg_ctx* c) {
   c->rot_cap = 3 * k * k;
   // test hook: a small log forces the overflow fallback path
   if (const char* env = getenv("LETKF_GB300_ROT_CAP")) c->rot_cap = std::max(1, atoi(env));
+  if (c->cubes) {
+    // cube solves: one buffer set of Gram matrices for a chunk of solves, and
+    // every solve's trans (the columns of a cube may take it from several)
+    int r = build_cube_plan(c);
+    if (r != LG_OK) return r;
+    c->cube_cs = (int)std::min<size_t>((size_t)c->cube_ns,
+                                       std::max<size_t>(1, budget / ((size_t)k * k * sizeof(double))));
+    lg_ctx::SolveLane& L = c->lane[0];
+    if (L.cap < (size_t)c->cube_cs) {
+      dfree(L.C); dfree(L.t); dfree(L.ovf_n);
+      L.cap = 0;
+      r |= dalloc(&L.C, (size_t)c->cube_cs * k * k);
+      r |= dalloc(&L.t, (size_t)c->cube_cs * k);
+      r |= dalloc(&L.ovf_n, 1);
+      if (r != LG_OK) return LG_ERR_NOMEM;
+      L.cap = (size_t)c->cube_cs;
+    }
+    if (c->trans_cap < (size_t)c->cube_ns) {
+      dfree(c->d_trans);
+      c->trans_cap = 0;
+      if (dalloc(&c->d_trans, (size_t)c->cube_ns * k * k) != LG_OK) return LG_ERR_NOMEM;
+      c->trans_cap = (size_t)c->cube_ns;
+    }
+    const int nq = (c->cube_ns + c->cube_cs - 1) / c->cube_cs;
+    while ((int)c->kev.size() < 7 * nq) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      c->kev.push_back(e);
+    }
+    c->capacity_ready = true;
+    return LG_OK;
+  }
   const int nl = c->tune.solve_streams;
   // rotation log entries: (cos, sin) as two doubles, or two floats where only
   // the FP32 vector kernel replays them (mixed precision)
@@ -987,6 +1078,59 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     rec.inv_dz = inv_dz;
   }
   CK(record_event(c->ev[2], st));
+  auto finish = [&]() -> int {
+    CK(record_event(c->ev[3], st));
+    if (io) {
+      // the copies not hidden behind the analysis
+      CK(record_event(c->ev_io[2], st));
+      CK(cudaEventRecord(c->ev_copy_join, c->copy_stream));
+      CK(cudaStreamWaitEvent(st, c->ev_copy_join, 0));
+      CK(record_event(c->ev_io[3], st));
+    }
+    CK(cudaGetLastError());
+    *launches_out = launches;
+    return LG_OK;
+  };
+  if (c->cubes) {
+    // Cube solves, on st: per chunk of solves the Gram at each solve's centre
+    // column and level (per-solve kernels) and the solve's explicit trans
+    // (FP64 eigensolver); then every column from the cubes that cover it.
+    const int cs = c->cube_cs, ns = c->cube_ns;
+    lg_ctx::SolveLane& L = c->lane[0];
+    for (int q = 0; q * cs < ns; ++q) {
+      cudaEvent_t* kv = &c->kev[7 * q];
+      lg::SolveBatch b{};
+      b.mode = 0;
+      b.levels = 1;
+      b.s_col = c->d_s_col;
+      b.s_kk = c->d_s_kk;
+      b.first_solve = q * cs;
+      b.nsolves = std::min(cs, ns - q * cs);
+      b.work = c->d_work;
+      CK(record_event(kv[0], st));
+      if (mixed_tc)
+        lg::launch_gram_tc_stream(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec, st);
+      else
+        lg::launch_gram64(geo, c->hx, c->lists, b, axb, L.C, L.t, st);
+      CK(record_event(kv[1], st));
+      CK(record_event(kv[2], st));
+      lg::launch_eig_apply(geo, b, L.C, L.t, xb, axb, xa, axa, c->d_trans, nullptr,
+                           c->d_status + 1, st);
+      for (int e = 3; e < 7; ++e) CK(record_event(kv[e], st));
+      launches += 2;
+    }
+    const lg::CubeDev cd{g.cube_n, g.cube_nz, g.cube_n - g.overlap, c->cube_ngroups,
+                         (g.vert_dist > 0.0 && g.overlap == 0) ? 1 : 0, c->d_cube_off};
+    lg::launch_cube_apply(geo, cd, c->d_trans, xb, axb, xa, axa, st);
+    launches += 1;
+    if (io) {
+      CK(cudaEventRecord(c->ev_phase[3][0], st));
+      CK(cudaStreamWaitEvent(c->copy_stream, c->ev_phase[3][0], 0));
+      CK(copy_cols_d2h(g, io->xa, xa, (size_t)c->geo.n * k, 0, ncol, c->copy_stream));
+      CK(copy_cols_d2h(g, io->axa, axa, (size_t)c->geo.n, 0, ncol, c->copy_stream));
+    }
+    return finish();
+  }
   const int levels = g.vert_dist > 0.0 ? g.nz : 1;
   const int chunk = c->chunk;
   const int nchunks = (ncol + chunk - 1) / chunk;
@@ -1133,17 +1277,7 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
       CK(cudaStreamWaitEvent(st, c->ev_join4, 0));
     }
   }
-  CK(record_event(c->ev[3], st));
-  if (io) {
-    // the copies not hidden behind the analysis
-    CK(record_event(c->ev_io[2], st));
-    CK(cudaEventRecord(c->ev_copy_join, c->copy_stream));
-    CK(cudaStreamWaitEvent(st, c->ev_copy_join, 0));
-    CK(record_event(c->ev_io[3], st));
-  }
-  CK(cudaGetLastError());
-  *launches_out = launches;
-  return LG_OK;
+  return finish();
 }
 
 }  // namespace
@@ -1204,7 +1338,8 @@ int run_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, dou
   CK(cudaMemcpyAsync(&band, c->d_band, sizeof(band), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&work, c->d_work, sizeof(work), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  const int nchunks = (ncol + c->chunk - 1) / c->chunk;
+  const int nchunks = c->cubes ? (c->cube_ns + c->cube_cs - 1) / c->cube_cs
+                               : (ncol + c->chunk - 1) / c->chunk;
   for (int q = 0; q < nchunks; ++q) {
     const cudaEvent_t* kv = &c->kev[7 * q];
     const float a = elapsed_ms(kv[0], kv[1]);
@@ -1225,7 +1360,7 @@ int run_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, dou
   S.n_launches = launches;
   S.n_gram_entries = (int64_t)work;
   S.n_columns = ncol;
-  S.n_solves = (int64_t)ncol * (g.vert_dist > 0.0 ? g.nz : 1);
+  S.n_solves = c->cubes ? (int64_t)c->cube_ns : (int64_t)ncol * (g.vert_dist > 0.0 ? g.nz : 1);
   S.n_copies = c->obs.n_copies;
   S.n_entries = c->obs.n_entries;
   S.nobsl_total = c->list_total;
@@ -1539,6 +1674,7 @@ void lg_destroy(lg_ctx* c) {
   }
   dfree(c->d_status); dfree(c->d_band);
   dfree(c->d_rec); dfree(c->d_boff);
+  dfree(c->d_cube_off); dfree(c->d_s_col); dfree(c->d_s_kk); dfree(c->d_trans);
   dfree(c->d_xb); dfree(c->d_axb); dfree(c->d_xa); dfree(c->d_axa);
   dfree(c->d_xin); dfree(c->d_spb); dfree(c->d_spa);
   for (auto& e : c->ev)

@@ -284,16 +284,18 @@ __global__ void __launch_bounds__(NT) eig_apply_kernel(Geometry g, SolveBatch b,
   __syncthreads();
   if (tid == 0) s_fail = 0;
 
-  if (b.mode == 1) {
-    // explicit trans(i, j) = W(i, j) + overline_w(i), column-major
-    double* T = trans_out + (size_t)s * n * n;
+  if (b.mode == 1 || b.s_col) {
+    // explicit trans(i, j) = W(i, j) + overline_w(i), column-major (cube
+    // solves: at the solve's index in the analysis; applied by the cube kernel)
+    const size_t so = b.s_col ? (size_t)b.first_solve + s : (size_t)s;
+    double* T = trans_out + so * n * n;
     for (int i = tid; i < n; i += NT) {
       for (int j = 0; j < n; ++j) {
         double w = 0.0;
         for (int m = 0; m < n; ++m) w += a[i * LD + m] * e[m] * a[j * LD + m];
         T[i + (size_t)n * j] = w + wb[i];
       }
-      wbar_out[(size_t)s * n + i] = wb[i];
+      if (wbar_out) wbar_out[so * n + i] = wb[i];
     }
     __syncthreads();
     continue;

@@ -49,8 +49,7 @@ __global__ void __launch_bounds__(kGramThreads) gram64_kernel(Geometry g, HxDev 
   int col = 0, kk = 1;
   bool vertical = false;
   if (b.mode == 0) {
-    col = b.first_col + s / b.levels;
-    kk = s % b.levels + 1;
+    solve_col_level(b, s, col, kk);
     base = l.off[col];
     p = l.cnt[col];
     vertical = g.vert_dist > 0.0;

@@ -59,8 +59,8 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev
   bool vertical = false;
   const bool use_rec = (b.mode == 0) && rec.r != nullptr;
   if (b.mode == 0) {
-    col = b.first_col + s / b.levels;
-    const int kk = s % b.levels + 1;
+    int kk;
+    solve_col_level(b, s, col, kk);
     base = l.off[col];
     p = l.cnt[col];
     vertical = g.vert_dist > 0.0;
@@ -337,8 +337,8 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_stream_kernel(Geometry g
   const int s = blockIdx.x;
   const int k = g.ens;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int col = b.first_col + s / b.levels;
-  const int kk = s % b.levels + 1;
+  int col, kk;
+  solve_col_level(b, s, col, kk);
   const int64_t base = l.off[col];
   const bool vertical = g.vert_dist > 0.0;
   if (tid == 0) {

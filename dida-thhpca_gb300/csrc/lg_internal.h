@@ -124,7 +124,24 @@ struct SolveBatch {
   // optional: process only the solves listed in solve_list[0 .. *solve_count)
   const int* solve_list;
   const int* solve_count;
+  // mode 0 with cubes: solve s of the batch is solve first_solve + s of the
+  // analysis, at centre column s_col[.] and centre level s_kk[.] (1-based);
+  // its trans goes to eig_apply's trans output
+  const int* s_col;
+  const int* s_kk;
+  int first_solve;
 };
+
+// column and level (1-based) of solve s of a mode-0 batch
+__host__ __device__ inline void solve_col_level(const SolveBatch& b, int s, int& col, int& kk) {
+  if (b.s_col) {
+    col = b.s_col[b.first_solve + s];
+    kk = b.s_kk[b.first_solve + s];
+  } else {
+    col = b.first_col + s / b.levels;
+    kk = s % b.levels + 1;
+  }
+}
 
 // kernels (host launchers), all asynchronous on `stream`
 // cand[slot] of every copy slot (slot_obs[slot] = observation of the slot)
@@ -169,6 +186,20 @@ void launch_gram_tc_stream(const Geometry& g, const HxDev& hx, const ListDev& l,
                            const RecDev& rec, cudaStream_t stream);
 void launch_records(int ncol, const ListDev& l, const HxDev& hx, float lo, float inv_dz, int nb,
                     int* boff, float4* rec, cudaStream_t stream);
+// Cube solves (da_block_interval cube_n, da_vertical_interval cube_nz,
+// da_block_overlap): cubes of cube_n x cube_n columns of a block, stepping by
+// stride = cube_n - overlap from each block's first column, numbered block by
+// block (longitude outer, latitude inner as the reference loops); solve
+// (cube, level group) = cube * ngroups + group.
+struct CubeDev {
+  int cube_n, cube_nz, stride, ngroups;
+  int grouped;          // vertical path without overlap: level groups of cube_nz levels
+  const int* cube_off;  // nblocks + 1: first cube of each block
+};
+void launch_cube_apply(const Geometry& g, const CubeDev& cd, const double* trans,
+                       const double* xb, const double* axb, double* xa, double* axa,
+                       cudaStream_t stream);
+
 void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
                       const double* xb, const double* axb, double* xa, double* axa,
                       double* trans, double* wbar, int* eig_fail, cudaStream_t stream);

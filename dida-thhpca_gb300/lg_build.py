@@ -29,6 +29,7 @@ UNITS = {
     "lg_eig2.cu": [],
     "lg_noalloc.cu": [],
     "lg_prepost.cu": [],
+    "lg_cube.cu": [],
 }
 
 

@@ -87,9 +87,14 @@ typedef struct lg_config {
   int max_obs;         /* MAX_OBS cap on local entries per column; 0 = no cap */
   int global_nx;       /* virtual decomposition: blocks in latitude */
   int global_ny;       /* virtual decomposition: blocks in longitude */
-  int cube_n;          /* da_block_interval; only 1 is supported */
-  int cube_nz;         /* da_vertical_interval; only 1 is supported */
-  int overlap;         /* da_block_overlap; only 0 is supported */
+  int cube_n;          /* da_block_interval: one solve per cube of cube_n x cube_n columns of
+                          a block, from the list of its centre column (>= 1) */
+  int cube_nz;         /* da_vertical_interval: one solve per cube_nz levels at their centre
+                          level (vertical localisation without overlap; >= 1) */
+  int overlap;         /* da_block_overlap, 0 <= overlap < cube_n: cubes step by
+                          cube_n - overlap and each column is the average over the cubes
+                          covering it; as in the reference this path has no vertical
+                          localisation (vert_dist is ignored) */
   int precision;       /* LG_PREC_FP64 or LG_PREC_MIXED */
   int vcoord;          /* LG_VCOORD_HYBRID or LG_VCOORD_SIGMA */
 } lg_config;

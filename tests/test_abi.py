@@ -37,8 +37,9 @@ def test_status_strings_and_null_arguments(built_lib):
     assert L.lg_create(None, None) == -1
     cfg = lg.preset("tiny2d").to_c()
     cfg.cube_n = 2
+    cfg.overlap = 2
     h = C.c_void_p()
-    assert L.lg_create(C.byref(h), C.byref(cfg)) == -3  # cube_n > 1 unsupported
+    assert L.lg_create(C.byref(h), C.byref(cfg)) == -1  # overlap >= cube_n: no step
     cfg = lg.preset("tiny2d").to_c()
     cfg.ens = 1
     assert L.lg_create(C.byref(h), C.byref(cfg)) == -1

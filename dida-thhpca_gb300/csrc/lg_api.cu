@@ -1612,6 +1612,50 @@ int lg_get_stats(const lg_ctx* c, lg_stats* st) {
   return LG_OK;
 }
 
+int lg_obs_from_records(int nz, int nvar, int n_records, const float* lon, const float* lat,
+                        const float* lev, const float* val, const float* noise, int max_obs,
+                        int* n_obs, double* lat_out, double* lon_out, double* ph_out,
+                        double* yo_out, double* rinv_out) {
+  if (nz < 1 || nz > 64 || nvar < 1 || nvar > LG_MAX_OBS_VARS || n_records < 0 || max_obs < 0 ||
+      !n_obs)
+    return LG_ERR_ARG;
+  if (n_records > 0 && (!lon || !lat || !lev || !val)) return LG_ERR_ARG;
+  if (max_obs > 0 && (!lat_out || !lon_out || !ph_out || !yo_out || !rinv_out)) return LG_ERR_ARG;
+  const int nval = 2 * nvar + 1;
+  int idx = -1;           // current observation
+  int next_level = 1;     // profiles: the level the next record must fill
+  for (int r = 0; r < n_records; ++r) {
+    const float lv = lev[r];
+    const int l = (int)lv;
+    if ((float)l != lv || l < 1 || l > nz) return LG_ERR_SHAPE;
+    if (l == 1) {
+      if (idx >= 0 && next_level != nz + 1) return LG_ERR_SHAPE;  // previous profile incomplete
+      ++idx;
+      if (idx >= max_obs) return LG_ERR_SHAPE;
+      lat_out[idx] = (double)lat[r];
+      lon_out[idx] = (double)lon[r];
+      next_level = 1;
+    }
+    if (idx < 0 || l != next_level) return LG_ERR_SHAPE;  // levels in order 1..nz
+    ++next_level;
+    const float* v = val + (size_t)r * nval;
+    ph_out[(size_t)idx * nz + (l - 1)] = (double)v[2 * nvar];
+    for (int n = 0; n < nvar; ++n) {
+      const float sd = v[2 * n + 1];
+      // REAL(4): val_buf(2n-1) + randn * val_buf(2n);  1.0 / val_buf(2n)**2
+      const float pert = noise ? noise[(size_t)n * n_records + r] * sd : 0.0f;
+      const float yo = v[2 * n] + pert;
+      const float ri = 1.0f / (sd * sd);
+      const size_t e = ((size_t)idx * nz + (l - 1)) * nvar + n;
+      yo_out[e] = (double)yo;
+      rinv_out[e] = (double)ri;
+    }
+  }
+  if (idx >= 0 && next_level != nz + 1) return LG_ERR_SHAPE;
+  *n_obs = idx + 1;
+  return LG_OK;
+}
+
 int lg_get_timeline(const lg_ctx* c, float* ms, int cap, int* nchunks) {
   if (!c || !nchunks || cap < 0) return LG_ERR_ARG;
   const int nq = (int)c->stats.n_chunks;

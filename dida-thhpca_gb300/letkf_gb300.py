@@ -270,6 +270,31 @@ def model_grid(cfg: Config):
 _lib = None
 
 
+def obs_from_records(nz: int, nvar: int, lon, lat, lev, val, noise=None):
+    """lg_obs_from_records: one type's observation records in the Redis store's
+    layout (val: records x (2*nvar+1) float32 -- value and error sd per
+    variable, then pressure) -> (lat, lon, ph, yo, rinv) arrays in the
+    lg_obs_soa layout of that type.  noise: (nvar, records) standard normals
+    for the perturbation, or None."""
+    lib = load_library()
+    f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    lon, lat, lev, val = f32(lon), f32(lat), f32(lev), f32(val)
+    nrec = lon.size
+    max_obs = nrec
+    out = [np.zeros(max(1, max_obs * m)) for m in (1, 1, nz, nz * nvar, nz * nvar)]
+    n = C.c_int()
+    nz_ = None if noise is None else f32(noise)
+    check(lib.lg_obs_from_records(nz, nvar, nrec, _ptr(lon, C.c_float), _ptr(lat, C.c_float),
+                                  _ptr(lev, C.c_float), _ptr(val, C.c_float),
+                                  None if nz_ is None else _ptr(nz_, C.c_float), max_obs,
+                                  C.byref(n), *[_ptr(a, C.c_double) for a in out]),
+          "lg_obs_from_records")
+    m = n.value
+    lat_o, lon_o, ph, yo, rinv = out
+    return (lat_o[:m], lon_o[:m], ph[:m * nz].reshape(m, nz), yo[:m * nz * nvar].reshape(m, nz, nvar),
+            rinv[:m * nz * nvar].reshape(m, nz, nvar))
+
+
 def load_library(path: str = LIB_PATH):
     """Load the compiled C ABI; raises if it has not been built."""
     global _lib
@@ -291,6 +316,8 @@ def load_library(path: str = LIB_PATH):
                                   C.c_void_p, C.c_void_p]
     lib.lg_get_stats.argtypes = [C.c_void_p, P(LgStats)]
     lib.lg_get_timeline.argtypes = [C.c_void_p, P(C.c_float), C.c_int, P(C.c_int)]
+    lib.lg_obs_from_records.argtypes = [C.c_int, C.c_int, C.c_int] + [P(C.c_float)] * 5 + [
+        C.c_int, P(C.c_int)] + [P(C.c_double)] * 5
     lib.lg_get_tuning.argtypes = [C.c_void_p, P(LgTuning)]
     lib.lg_set_tuning.argtypes = [C.c_void_p, P(LgTuning)]
     lib.lg_autotune.argtypes = [C.c_void_p] + [C.c_void_p] * 5 + [P(LgTuning)]

@@ -197,6 +197,27 @@ int lg_run_da_parallel(lg_ctx* ctx, int ntimes, double gamma1, double gamma2, do
                        const double* xb_in, double* xa_out, double* spread_b,
                        double* spread_a);
 
+/* Observation records of one type as the reference's Redis observation store
+ * returns them (RedisGetobserveF), reshaped as read_obs does
+ * (x86/DA/LETKF/src/read_obs_mod.F90:338-449) into this library's observation
+ * arrays.  Record r has lon[r], lat[r], lev[r] (1-based level) and 2*nvar+1
+ * floats at val[r*(2*nvar+1)]: value and error sd of each variable in turn,
+ * then the pressure [Pa].  nz == 1: one observation per record.  nz > 1
+ * (profiles such as ADPUPA, GPSRO): a record with lev == 1 starts an
+ * observation and gives its position, and each record fills level lev; every
+ * level of every profile must be present (LG_ERR_SHAPE otherwise, as a missing
+ * level would leave a zero pressure).  The observed value is perturbed as
+ * read_obs does, value + noise * sd in REAL(4), with caller-supplied standard
+ * normal noise[v * n_records + r] for variable v of record r (NULL: no
+ * perturbation); rinv = 1 / sd^2 in REAL(4).  Outputs, caller-allocated for
+ * max_obs observations: lat, lon (n_obs), ph (n_obs*nz), yo and rinv
+ * (n_obs*nz*nvar, variable fastest, then level) -- the lg_obs_soa layout of one
+ * type; *n_obs receives the count.  Host only; needs no device. */
+int lg_obs_from_records(int nz, int nvar, int n_records, const float* lon, const float* lat,
+                        const float* lev, const float* val, const float* noise, int max_obs,
+                        int* n_obs, double* lat_out, double* lon_out, double* ph_out,
+                        double* yo_out, double* rinv_out);
+
 /* Statistics of the last lg_run. */
 int lg_get_stats(const lg_ctx* ctx, lg_stats* st);
 

@@ -200,6 +200,11 @@ void launch_cube_apply(const Geometry& g, const CubeDev& cd, const double* trans
                        const double* xb, const double* axb, double* xa, double* axa,
                        cudaStream_t stream);
 
+cudaError_t launch_gmcore_to_da(int ens, int num_lat, int num_lon, int nz, int halo,
+                                const double* ps, const double* u_half, const double* v_half,
+                                const double* pt, const double* area_subcell,
+                                const double* area_cell, double* xb, cudaStream_t stream);
+
 void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, const double* t,
                       const double* xb, const double* axb, double* xa, double* axa,
                       double* trans, double* wbar, int* eig_fail, cudaStream_t stream);

@@ -270,6 +270,26 @@ def model_grid(cfg: Config):
 _lib = None
 
 
+def gmcore_to_da(ps, u_half, v_half, pt, area_subcell, area_cell, halo: int, stream=None):
+    """lg_gmcore_to_da_device on torch CUDA float64 tensors (members last):
+    ps [lat, lon, ens], u_half [nz, lat, lon, ens], v_half [nz, lat + 1, lon, ens],
+    pt [nz, lat, lon, ens], area_subcell [lat, 2], area_cell [lat] -> the DA
+    background xb [lon + 2 halo, lat + 2 halo, 1 + 3 nz, ens] (latitude halo
+    rows zero)."""
+    import torch
+    lib = load_library()
+    nz, num_lat, num_lon, ens = u_half.shape
+    xb = torch.zeros((num_lon + 2 * halo, num_lat + 2 * halo, 1 + 3 * nz, ens),
+                     dtype=torch.float64, device=ps.device)
+    args = [t.contiguous() for t in (ps, u_half, v_half, pt, area_subcell, area_cell)]
+    check(lib.lg_gmcore_to_da_device(ens, num_lat, num_lon, nz, halo,
+                                     *[C.c_void_p(t.data_ptr()) for t in args],
+                                     C.c_void_p(xb.data_ptr()),
+                                     C.c_void_p(stream) if stream is not None else None),
+          "lg_gmcore_to_da_device")
+    return xb
+
+
 def obs_from_records(nz: int, nvar: int, lon, lat, lev, val, noise=None):
     """lg_obs_from_records: one type's observation records in the Redis store's
     layout (val: records x (2*nvar+1) float32 -- value and error sd per
@@ -316,6 +336,7 @@ def load_library(path: str = LIB_PATH):
                                   C.c_void_p, C.c_void_p]
     lib.lg_get_stats.argtypes = [C.c_void_p, P(LgStats)]
     lib.lg_get_timeline.argtypes = [C.c_void_p, P(C.c_float), C.c_int, P(C.c_int)]
+    lib.lg_gmcore_to_da_device.argtypes = [C.c_int] * 5 + [C.c_void_p] * 8
     lib.lg_obs_from_records.argtypes = [C.c_int, C.c_int, C.c_int] + [P(C.c_float)] * 5 + [
         C.c_int, P(C.c_int)] + [P(C.c_double)] * 5
     lib.lg_get_tuning.argtypes = [C.c_void_p, P(LgTuning)]

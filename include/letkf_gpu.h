@@ -218,6 +218,26 @@ int lg_obs_from_records(int nz, int nvar, int n_records, const float* lon, const
                         int* n_obs, double* lat_out, double* lon_out, double* ph_out,
                         double* yo_out, double* rinv_out);
 
+/* GMCORE state of all members to the DA background layout, on the device (the
+ * coupler step before run_da_parallel: gmcore2da_send_coupling,
+ * x86/ATM/gmcore_mct/gmcore_coupler.F90:153-284, and the receive into
+ * xb(ens, n, lat, lon), x86/DA/EnDNN/src/module_da_coupler.F90:91-147,350-414).
+ * Inputs, members fastest (GMCORE's (member, lon, lat, lev) arrays):
+ *   ps           [lat][lon][ens]
+ *   u_half       [nz][lat][lon][ens]    u_f: u east of each full longitude (C grid)
+ *   v_half       [nz][lat + 1][lon][ens] v_f at half latitudes 0..num_lat (C grid)
+ *   pt           [nz][lat][lon][ens]
+ *   area_subcell [lat][2], area_cell [lat]  (GMCORE mesh; device arrays)
+ * Output xb [lon + 2 halo][lat + 2 halo][1 + 3 nz][ens] (the lg_run layout with
+ * rows ps, u, v, pt): u = (u_f(i) + u_f(i-1)) / 2 (periodic),
+ * v = 2 (v_f(j-1) area_subcell(1,j) + v_f(j) area_subcell(2,j)) / area_cell(j);
+ * the longitude halo is filled periodically, latitude halo rows are not
+ * written.  Enqueued on stream (NULL: the default stream); no synchronisation. */
+int lg_gmcore_to_da_device(int ens, int num_lat, int num_lon, int nz, int halo,
+                           const double* d_ps, const double* d_u_half, const double* d_v_half,
+                           const double* d_pt, const double* d_area_subcell,
+                           const double* d_area_cell, double* d_xb, void* stream);
+
 /* Statistics of the last lg_run. */
 int lg_get_stats(const lg_ctx* ctx, lg_stats* st);
 

@@ -803,6 +803,12 @@ float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
 // groups (cube_nz levels on the vertical path, :431-436): the centre column
 // ((sj + ej) / 2, (si + ei) / 2) and centre level ((sk + ek) / 2) of every solve.
 // Fixed by the grid and configuration, so built once per context.
+// mixed precision cube solves form their trans in FP32 from the tridiagonal
+// form and the QL rotation log (trans_kernel); FP64 ones with eig_apply
+bool cube_trans_fp32(const lg_ctx* c) {
+  return c->cfg.precision == LG_PREC_MIXED && c->cfg.ens <= 64;
+}
+
 int build_cube_plan(lg_ctx* c) {
   if (c->cube_plan) return LG_OK;
   const lg_config& g = c->cfg;
@@ -910,14 +916,28 @@ int prepare_capacity(lg_ctx* c) {
     c->cube_cs = (int)std::min<size_t>((size_t)c->cube_ns,
                                        std::max<size_t>(1, budget / ((size_t)k * k * sizeof(double))));
     lg_ctx::SolveLane& L = c->lane[0];
-    if (L.cap < (size_t)c->cube_cs) {
-      dfree(L.C); dfree(L.t); dfree(L.ovf_n);
+    // mixed precision: tridiagonal form and rotation log for the FP32 trans
+    const bool eig2 = cube_trans_fp32(c);
+    if (L.cap < (size_t)c->cube_cs || L.rot_n_cap != (eig2 ? (size_t)c->rot_cap : 0)) {
+      dfree(L.C); dfree(L.t); dfree(L.tri); dfree(L.lam); dfree(L.rot_cs); dfree(L.rot_i);
+      dfree(L.rot_n); dfree(L.ovf_list); dfree(L.ovf_n);
       L.cap = 0;
-      r |= dalloc(&L.C, (size_t)c->cube_cs * k * k);
-      r |= dalloc(&L.t, (size_t)c->cube_cs * k);
+      L.rot_n_cap = 0;
+      const size_t cap = (size_t)c->cube_cs;
+      r |= dalloc(&L.C, cap * k * k);
+      r |= dalloc(&L.t, cap * k);
       r |= dalloc(&L.ovf_n, 1);
+      if (eig2) {
+        r |= dalloc(&L.tri, cap * lg::eig2_tri_doubles(k));
+        r |= dalloc(&L.lam, cap * k);
+        r |= dalloc(&L.rot_cs, (cap * (size_t)c->rot_cap + 1) / 2);  // float2 entries
+        r |= dalloc(&L.rot_i, cap * (size_t)c->rot_cap);
+        r |= dalloc(&L.rot_n, cap);
+        r |= dalloc(&L.ovf_list, cap);
+      }
       if (r != LG_OK) return LG_ERR_NOMEM;
-      L.cap = (size_t)c->cube_cs;
+      L.cap = cap;
+      L.rot_n_cap = eig2 ? (size_t)c->rot_cap : 0;
     }
     if (c->trans_cap < (size_t)c->cube_ns) {
       dfree(c->d_trans);
@@ -1114,10 +1134,29 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
         lg::launch_gram64(geo, c->hx, c->lists, b, axb, L.C, L.t, st);
       CK(record_event(kv[1], st));
       CK(record_event(kv[2], st));
-      lg::launch_eig_apply(geo, b, L.C, L.t, xb, axb, xa, axa, c->d_trans, nullptr,
-                           c->d_status + 1, st);
-      for (int e = 3; e < 7; ++e) CK(record_event(kv[e], st));
-      launches += 2;
+      if (cube_trans_fp32(c)) {
+        CK(cudaMemsetAsync(L.ovf_n, 0, sizeof(int), st));
+        lg::launch_eig2(geo, b, L.C, L.t, xb, axb, xa, axa, L.tri, L.lam, L.rot_cs, L.rot_i,
+                        L.rot_n, c->rot_cap, L.ovf_list, L.ovf_n, c->d_status + 1, true,
+                        c->tune.ql_warps, c->tune.vec_warps, lg::kEigTridiag | lg::kEigQL, st,
+                        kv[3], kv[4]);
+        CK(record_event(kv[5], st));
+        lg::launch_trans(geo, b, L.t, L.tri, L.lam, L.rot_cs, L.rot_i, L.rot_n, c->rot_cap,
+                         c->d_trans, st);
+        // solves the QL left to the FP64 solver (log overflow, FP32 reflector range)
+        lg::SolveBatch fb = b;
+        fb.solve_list = L.ovf_list;
+        fb.solve_count = L.ovf_n;
+        lg::launch_eig_apply(geo, fb, L.C, L.t, xb, axb, xa, axa, c->d_trans, nullptr,
+                             c->d_status + 1, st);
+        CK(record_event(kv[6], st));
+        launches += 5;
+      } else {
+        lg::launch_eig_apply(geo, b, L.C, L.t, xb, axb, xa, axa, c->d_trans, nullptr,
+                             c->d_status + 1, st);
+        for (int e = 3; e < 7; ++e) CK(record_event(kv[e], st));
+        launches += 2;
+      }
     }
     const lg::CubeDev cd{g.cube_n, g.cube_nz, g.cube_n - g.overlap, c->cube_ngroups,
                          (g.vert_dist > 0.0 && g.overlap == 0) ? 1 : 0, c->d_cube_off};

@@ -586,6 +586,97 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
 #undef YY
 }
 
+// ---------------------------------------------------------------- explicit trans
+// Mixed path, cube solves: trans(i, j) = sqrt(rho) [i == j] + D(i, j) + wbar(i)
+// (column-major, as letkf_core returns it) with the deviation
+// D = V diag(f - sqrt(rho)) V^T and wbar = V diag(1/lambda) V^T t, formed by
+// the vector pipeline of vec_kernel in FP32 -- FP32 reflectors, the rotation
+// log, the eigenvalue factors -- on t (thread 0) and the unit vectors e_j
+// (thread j + 1), one block per solve.  A solve whose rotation log overflowed
+// or whose reflectors left the FP32 range (rot_n < 0) is skipped: the FP64
+// fallback forms its trans.
+__global__ void __launch_bounds__(128) trans_kernel(int n, SolveBatch b, const double* tin,
+                                                    const double* tri, const double* lam,
+                                                    const float2* rot_cs,
+                                                    const unsigned char* rot_i, const int* rot_n,
+                                                    int rot_cap, double srho, double* trans_out) {
+  const int s = blockIdx.x;
+  const int nt = blockDim.x, v = threadIdx.x;
+  const int nrot = rot_n[s];
+  if (nrot < 0) return;  // the whole block: the FP64 fallback forms this trans
+  extern __shared__ float yt[];  // n x nt, [i][thread]
+#define YV(i) yt[(i) * nt + v]
+  const double* T = tri + (size_t)s * e2::tri_stride(n);
+  const float2* fl = reinterpret_cast<const float2*>(lam + (size_t)s * n);
+  if (v <= n) {
+    if (v == 0) {
+      for (int i = 0; i < n; ++i) YV(i) = d2f_bits(tin[(size_t)s * n + i]);
+    } else {
+      for (int i = 0; i < n; ++i) YV(i) = (i == v - 1) ? 1.0f : 0.0f;
+    }
+    const float* U32 = reinterpret_cast<const float*>(T + 3 * n);
+    const float* Act32 = U32 + (size_t)n * (n - 1) / 2;
+    // y = Q^T x (P_{n-1} first)
+    for (int i = n - 1; i >= 1; --i) {
+      if (Act32[i] == 0.0f) continue;
+      const float* u = U32 + e2::uoff(i);
+      float dot = 0.0f;
+      for (int kk = 0; kk < i; ++kk) dot += u[kk] * YV(kk);
+      for (int kk = 0; kk < i; ++kk) YV(kk) -= u[kk] * dot;
+    }
+    // y = Z^T y: rotations in generation order
+    const float2* cs = rot_cs + (size_t)s * rot_cap;
+    const unsigned char* ix = rot_i + (size_t)s * rot_cap;
+    for (int r = 0; r < nrot; ++r) {
+      const float2 c = cs[r];
+      const int i = ix[r];
+      const float a0 = YV(i), a1 = YV(i + 1);
+      YV(i) = c.x * a0 - c.y * a1;
+      YV(i + 1) = c.y * a0 + c.x * a1;
+    }
+    // 1/lambda for t, f - sqrt(rho) for the unit vectors
+    for (int j = 0; j < n; ++j) YV(j) *= (v == 0) ? fl[j].x : fl[j].y;
+    // y = Z y: rotations in reverse order
+    for (int r = nrot - 1; r >= 0; --r) {
+      const float2 c = cs[r];
+      const int i = ix[r];
+      const float a0 = YV(i), a1 = YV(i + 1);
+      YV(i) = c.x * a0 + c.y * a1;
+      YV(i + 1) = -c.y * a0 + c.x * a1;
+    }
+    // y = Q y (P_1 first)
+    for (int i = 1; i < n; ++i) {
+      if (Act32[i] == 0.0f) continue;
+      const float* u = U32 + e2::uoff(i);
+      float dot = 0.0f;
+      for (int kk = 0; kk < i; ++kk) dot += u[kk] * YV(kk);
+      for (int kk = 0; kk < i; ++kk) YV(kk) -= u[kk] * dot;
+    }
+  }
+#undef YV
+  __syncthreads();
+  double* To = trans_out + ((size_t)b.first_solve + s) * n * n;
+  for (int idx = v; idx < n * n; idx += nt) {
+    const int i = idx % n, j = idx / n;
+    double val = f2d_bits(yt[i * nt + j + 1]) + f2d_bits(yt[i * nt]);
+    if (i == j) val += srho;
+    To[idx] = val;
+  }
+}
+
+void launch_trans(const Geometry& g, const SolveBatch& b, const double* t, const double* tri,
+                  const double* lam, const void* rot_cs, const unsigned char* rot_i,
+                  const int* rot_n, int rot_cap, double* trans, cudaStream_t stream) {
+  const int n = g.ens;
+  if (b.nsolves == 0) return;
+  const int nt = ((n + 1 + 31) / 32) * 32;
+  const size_t smem = sizeof(float) * (size_t)n * nt;
+  cudaFuncSetAttribute(trans_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  trans_kernel<<<b.nsolves, nt, smem, stream>>>(n, b, t, tri, lam,
+                                                static_cast<const float2*>(rot_cs), rot_i, rot_n,
+                                                rot_cap, sqrt(g.inflation), trans);
+}
+
 // ------------------------------------------------------------ host launchers
 size_t eig2_tri_doubles(int n) { return (size_t)n * (n + 3); }
 

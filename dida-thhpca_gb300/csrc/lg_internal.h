@@ -210,6 +210,11 @@ void launch_eig_apply(const Geometry& g, const SolveBatch& b, const double* C, c
                       double* trans, double* wbar, int* eig_fail, cudaStream_t stream);
 size_t eig2_tri_doubles(int n);
 bool eig2_supported(const Geometry& g);
+// mixed path, cube solves: explicit trans of each solve from the tridiagonal
+// form and rotation log (solves with rot_n < 0 are left to eig_apply)
+void launch_trans(const Geometry& g, const SolveBatch& b, const double* t, const double* tri,
+                  const double* lam, const void* rot_cs, const unsigned char* rot_i,
+                  const int* rot_n, int rot_cap, double* trans, cudaStream_t stream);
 // phases of launch_eig2 (a bit mask)
 constexpr int kEigTridiag = 1, kEigQL = 2, kEigVectors = 4, kEigAll = 7;
 void launch_eig2(const Geometry& g, const SolveBatch& b, const double* C, const double* t,

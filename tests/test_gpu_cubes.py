@@ -80,3 +80,25 @@ def test_cube_analysis_mixed_within_tolerance(name, over):
     errs = increment_rel_rms(cfg, w, (xa, axa), (xa_o, axa_o))
     assert max(errs.values()) <= TOL_INCREMENT, errs
     ctx.letkf_final()
+
+
+def test_cube_mixed_fallback_for_overflowed_rotation_logs(monkeypatch):
+    """Mixed cube solves whose QL rotation log overflows get their trans from
+    the FP64 solver instead of the FP32 pipeline: a 50-entry log sends almost
+    every solve there, and the analysis stays within the tolerance."""
+    import letkf_gb300 as lg
+    import synth
+    from test_gpu_mixed import TOL_INCREMENT, increment_rel_rms
+    monkeypatch.setenv("LETKF_GB300_ROT_CAP", "50")
+    base = lg.preset("tiny3d").replace(cube_n=2)
+    cfg = base.replace(precision=lg.LG_PREC_MIXED)
+    w = synth.make_workload(cfg)
+    xa_o, axa_o, _ = _oracle(base, w)
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    xa = np.zeros_like(w.xb)
+    axa = np.zeros_like(w.axb)
+    ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+    errs = increment_rel_rms(cfg, w, (xa, axa), (xa_o, axa_o))
+    assert max(errs.values()) <= TOL_INCREMENT, errs
+    ctx.letkf_final()

@@ -158,6 +158,8 @@ __global__ void __launch_bounds__(128) hx_kernel(Geometry g, ObsDev ob, const do
   int jj[kMaxMemberSlots];
 #pragma unroll
   for (int q = 0; q < kMaxMemberSlots; ++q) jj[q] = 1;
+  bool has3d = false;  // the log-p weights are needed only for 3-D variables
+  for (int kv = 0; kv < onv; ++kv) has3d |= g.var_lev[c_types.var[ti][kv]] > 1;
   for (int l = 0; l < onz; ++l) {
     const double po = oph[l];
     const double lnpo = log(po);
@@ -169,6 +171,20 @@ __global__ void __launch_bounds__(128) hx_kernel(Geometry g, ObsDev ob, const do
         while (jj[q] <= g.nz && po > half_ph(g, jj[q], ps[q])) jj[q]++;
       }
       pp[q] = jj[q] - 1;
+    }
+    // vertical interpolation weight in log p of each member for this level,
+    // shared by the level's variables
+    double t3[kMaxMemberSlots];
+#pragma unroll
+    for (int q = 0; q < kMaxMemberSlots; ++q) {
+      const int e = (int)lane + 32 * q;
+      const int p = pp[q];
+      t3[q] = 0.0;
+      if (has3d && e < k && p >= 1 && p < g.nz) {
+        const double php1 = half_ph(g, p + 1, ps[q]), php = half_ph(g, p, ps[q]);
+        const double lp1 = log(php1);
+        t3[q] = __ddiv_rn(__dsub_rn(lp1, lnpo), __dsub_rn(lp1, log(php)));
+      }
     }
     for (int kv = 0; kv < onv; ++kv) {
       const int vid = c_types.var[ti][kv];
@@ -184,12 +200,9 @@ __global__ void __launch_bounds__(128) hx_kernel(Geometry g, ObsDev ob, const do
           const int p = pp[q];
           if (p >= 1 && p < g.nz) {
             const int tl = vs + p - 1;
-            const double php1 = half_ph(g, p + 1, ps[q]), php = half_ph(g, p, ps[q]);
-            const double lp1 = log(php1);
-            const double t3 = __ddiv_rn(__dsub_rn(lp1, lnpo), __dsub_rn(lp1, log(php)));
             const double r1 = bilin(xb, axb, k, n, e, tl, c11, c21, c12, c22, t1, t2);
             const double r3 = bilin(xb, axb, k, n, e, tl + 1, c11, c21, c12, c22, t1, t2);
-            y[q] = __dadd_rn(__dmul_rn(r1, t3), __dmul_rn(r3, __dsub_rn(1.0, t3)));
+            y[q] = __dadd_rn(__dmul_rn(r1, t3[q]), __dmul_rn(r3, __dsub_rn(1.0, t3[q])));
           } else {
             const int tl = (p == 0) ? vs : vs + g.nz - 1;
             y[q] = bilin(xb, axb, k, n, e, tl, c11, c21, c12, c22, t1, t2);
@@ -198,16 +211,15 @@ __global__ void __launch_bounds__(128) hx_kernel(Geometry g, ObsDev ob, const do
           y[q] = bilin(xb, axb, k, n, e, vs, c11, c21, c12, c22, t1, t2);
         }
       }
-      // sequential member sum in member order (letkf_obs.F90:160-164)
+      // member mean (letkf_obs.F90:160-164): per-lane partial sums over the
+      // member slots, then a shuffle tree (the reference sums in member order;
+      // the two agree to rounding, far inside the 1e-12 parity bound)
       double sum_y = 0.0;
 #pragma unroll
-      for (int q = 0; q < kMaxMemberSlots; ++q) {
-        if (32 * q >= k) break;
-        for (int src = 0; src < 32; ++src) {
-          double v = __shfl_sync(0xffffffffu, y[q], src);
-          if (32 * q + src < k) sum_y = __dadd_rn(sum_y, v);
-        }
-      }
+      for (int q = 0; q < kMaxMemberSlots; ++q)
+        if ((int)lane + 32 * q < k) sum_y = __dadd_rn(sum_y, y[q]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sum_y = __dadd_rn(sum_y, __shfl_xor_sync(0xffffffffu, sum_y, o));
       sum_y = __ddiv_rn(sum_y, (double)k);
 #pragma unroll
       for (int q = 0; q < kMaxMemberSlots; ++q) {

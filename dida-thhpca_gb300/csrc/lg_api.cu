@@ -113,7 +113,7 @@ struct lg_ctx {
   bool cube_plan = false;
   int cube_ns = 0, cube_cs = 1, cube_ngroups = 1;  // solves, solves per chunk, level groups
   int* d_cube_off = nullptr;
-  int *d_s_col = nullptr, *d_s_kk = nullptr;
+  int *d_s_col = nullptr, *d_s_kk = nullptr, *d_centres = nullptr;
   double* d_trans = nullptr;
   size_t trans_cap = 0;
   bool use_eig2 = false;
@@ -836,11 +836,19 @@ int build_cube_plan(lg_ctx* c) {
       }
     }
   }
+  // the distinct centre columns: the selection builds only their lists
+  std::vector<int> centres(s_col);
+  std::sort(centres.begin(), centres.end());
+  centres.erase(std::unique(centres.begin(), centres.end()), centres.end());
   int r = LG_OK;
   r |= dalloc(&c->d_cube_off, off.size());
   r |= dalloc(&c->d_s_col, s_col.size());
   r |= dalloc(&c->d_s_kk, s_kk.size());
+  r |= dalloc(&c->d_centres, centres.size());
   if (r != LG_OK) return LG_ERR_NOMEM;
+  CK(cudaMemcpy(c->d_centres, centres.data(), sizeof(int) * centres.size(), cudaMemcpyHostToDevice));
+  c->lists.col_list = c->d_centres;
+  c->lists.n_list = (int)centres.size();
   CK(cudaMemcpy(c->d_cube_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->d_s_col, s_col.data(), sizeof(int) * s_col.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->d_s_kk, s_kk.data(), sizeof(int) * s_kk.size(), cudaMemcpyHostToDevice));
@@ -865,6 +873,11 @@ int prepare_capacity(lg_ctx* c) {
     c->scan_tmp_bytes = lg::scan_tmp_bytes(ncol);
     r |= dalloc((char**)&c->d_scan_tmp, c->scan_tmp_bytes);
     if (r != LG_OK) return LG_ERR_NOMEM;
+  }
+  if (c->cubes) {
+    // the cube plan first: only the cube centres' lists are built
+    const int r = build_cube_plan(c);
+    if (r != LG_OK) return r;
   }
   CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
   if (c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH"))
@@ -1769,7 +1782,7 @@ void lg_destroy(lg_ctx* c) {
   }
   dfree(c->d_status); dfree(c->d_band);
   dfree(c->d_rec); dfree(c->d_boff);
-  dfree(c->d_cube_off); dfree(c->d_s_col); dfree(c->d_s_kk); dfree(c->d_trans);
+  dfree(c->d_cube_off); dfree(c->d_s_col); dfree(c->d_s_kk); dfree(c->d_trans); dfree(c->d_centres);
   dfree(c->d_xb); dfree(c->d_axb); dfree(c->d_xa); dfree(c->d_axa);
   dfree(c->d_xin); dfree(c->d_spb); dfree(c->d_spa);
   for (auto& e : c->ev)

@@ -96,6 +96,10 @@ struct ListDev {
   int* ent;          // total entries
   double* rloc;      // total entries
   int* capped;       // columns (1 if truncated at max_obs)
+  // selection only: build the lists of these columns alone (cube centres);
+  // the counts of the others stay as they are (zero)
+  const int* col_list = nullptr;
+  int n_list = 0;
 };
 
 // Per-column entry records grouped by ln p bucket (mixed-precision Gram input).

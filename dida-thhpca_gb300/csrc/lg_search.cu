@@ -27,9 +27,10 @@ struct SearchArgs {
 
 __global__ void __launch_bounds__(256) search_kernel(Geometry g, ObsDev ob, ListDev l, int fill,
                                                      SearchArgs sa, unsigned long long* band) {
-  const int col = blockIdx.x * (blockDim.x / 32) + (threadIdx.x / 32);
+  const int idx = blockIdx.x * (blockDim.x / 32) + (threadIdx.x / 32);
   const int ncol = g.num_lat * g.num_lon;
-  if (col >= ncol) return;
+  if (idx >= (l.col_list ? l.n_list : ncol)) return;
+  const int col = l.col_list ? l.col_list[idx] : idx;
   const unsigned lane = threadIdx.x & 31u;
   const int glat = col % g.num_lat + 1, glon = col / g.num_lat + 1;
   const int b = g.lon_block[glon - 1] * g.global_nx + g.lat_block[glat - 1];
@@ -126,7 +127,9 @@ void launch_search(const Geometry& g, const ObsDev& o, ListDev l, int fill,
     sa.vhi = (float)(v + 1e-5);
   }
   const int warps = 8;
-  search_kernel<<<(ncol + warps - 1) / warps, 32 * warps, 0, stream>>>(g, o, l, fill, sa, band);
+  const int nc = l.col_list ? l.n_list : ncol;
+  if (nc == 0) return;
+  search_kernel<<<(nc + warps - 1) / warps, 32 * warps, 0, stream>>>(g, o, l, fill, sa, band);
 }
 
 size_t scan_tmp_bytes(int n) {
@@ -294,11 +297,12 @@ __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob
                                                            unsigned long long* band) {
   const int warps = blockDim.x / 32;
   const int w = threadIdx.x >> 5;
-  const int col = blockIdx.x * warps + w;
+  const int idx = blockIdx.x * warps + w;
   const int ncol = g.num_lat * g.num_lon;
   extern __shared__ unsigned int bitmap_all[];
   unsigned int* bitmap = bitmap_all + (size_t)w * ci.bitmap_words;
-  if (col >= ncol) return;
+  if (idx >= (l.col_list ? l.n_list : ncol)) return;
+  const int col = l.col_list ? l.col_list[idx] : idx;
   const unsigned lane = threadIdx.x & 31u;
   const int glat = col % g.num_lat + 1, glon = col / g.num_lat + 1;
   const int b = g.lon_block[glon - 1] * g.global_nx + g.lat_block[glat - 1];
@@ -481,7 +485,9 @@ void launch_search_cells(const Geometry& g, const ObsDev& o, const CellIndex& ci
   const size_t smem = sizeof(unsigned int) * (size_t)warps * ci.bitmap_words;
   cudaFuncSetAttribute(search_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem);
-  search_cells_kernel<<<(ncol + warps - 1) / warps, 32 * warps, smem, stream>>>(g, o, ci, l, fill,
+  const int nc = l.col_list ? l.n_list : ncol;
+  if (nc == 0) return;
+  search_cells_kernel<<<(nc + warps - 1) / warps, 32 * warps, smem, stream>>>(g, o, ci, l, fill,
                                                                                  sa, band);
 }
 

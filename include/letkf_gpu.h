@@ -297,7 +297,8 @@ int lg_autotune(lg_ctx* ctx, const double* d_xb, const double* d_axb, double* d_
  * counts: num_lat*num_lon ints, column c = (lon-1)*num_lat + (lat-1);
  * entries/rloc: total local entries in column order; entries hold the global
  * copy-entry index (see lg_copy_layout).  Pass NULL arrays to query the total
- * through *total only. */
+ * through *total only.  With cubes only the cube centres' lists are built (the
+ * other columns count 0), and lg_stats.nobsl_total sums over those. */
 int lg_get_lists(const lg_ctx* ctx, int* counts, int* entries, double* rloc, int64_t* total);
 
 /* Layout of block-observation copies built by lg_set_obs: for each copy j

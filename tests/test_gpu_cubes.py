@@ -102,3 +102,27 @@ def test_cube_mixed_fallback_for_overflowed_rotation_logs(monkeypatch):
     errs = increment_rel_rms(cfg, w, (xa, axa), (xa_o, axa_o))
     assert max(errs.values()) <= TOL_INCREMENT, errs
     ctx.letkf_final()
+
+
+def test_cube_lists_only_at_centres():
+    """With cubes the selection builds only the cube centres' lists; each one
+    equals the oracle's list of that column."""
+    import letkf_gb300 as lg
+    import synth
+    from oracle import oracle as orc
+    cfg = lg.preset("tiny3d").replace(cube_n=3)
+    w = synth.make_workload(cfg)
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    xa = np.zeros_like(w.xb)
+    axa = np.zeros_like(w.axb)
+    ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+    counts, ent, _ = ctx.lists()
+    o = orc.Oracle(cfg, w.obs)
+    off = np.concatenate([[0], np.cumsum(counts)])
+    nz_cols = np.nonzero(counts)[0]
+    assert 0 < nz_cols.size < cfg.num_lat * cfg.num_lon // 4
+    for col in nz_cols[:: max(1, nz_cols.size // 12)]:
+        e_o, _ = o.column_list(int(col))
+        assert np.array_equal(ent[off[col]:off[col + 1]], e_o)
+    ctx.letkf_final()

@@ -126,3 +126,26 @@ def test_cube_lists_only_at_centres():
         e_o, _ = o.column_list(int(col))
         assert np.array_equal(ent[off[col]:off[col + 1]], e_o)
     ctx.letkf_final()
+
+
+@pytest.mark.parametrize("over", [dict(cube_n=3, overlap=1), dict(cube_n=2, cube_nz=3)])
+def test_cube_host_run_pinned_matches_pageable(over):
+    """lg_run with page-locked host arrays on the cube path (copies inside the
+    captured analysis) equals the pageable-array path bit for bit."""
+    import torch
+
+    import letkf_gb300 as lg
+    import synth
+    cfg = lg.preset("tiny3d").replace(**over)
+    w = synth.make_workload(cfg)
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    xa = np.full_like(w.xb, 3.0)
+    axa = np.full_like(w.axb, 3.0)
+    ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+    pin = [torch.from_numpy(a).pin_memory() for a in (w.xb, w.axb)]
+    out = [torch.full(a.shape, 3.0, dtype=torch.float64).pin_memory() for a in (w.xb, w.axb)]
+    pxb, paxb, pxa, paxa = (t.numpy() for t in pin + out)
+    ctx.letkf_run(0, pxb, paxb, pxa, paxa)
+    assert np.array_equal(pxa, xa) and np.array_equal(paxa, axa)
+    ctx.letkf_final()

@@ -663,15 +663,21 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
   d.dcx = dcx; d.dsx = dsx; d.dyr = dyr; d.fcx = fcx; d.fsx = fsx; d.fyr = fyr;
   lg::launch_obs_trig(d, dcx, dsx, dyr, fcx, fsx, fyr, c->own_stream);
   {
-    double lo = 1e300, hi = -1e300;
+    // ln p range of the observations (log is monotonic: the logs of the
+    // smallest and largest positive pressures)
+    double pmin = 1e300, pmax = -1.0;
     for (int64_t i = 0; i < ph_off[n]; ++i) {
       const double v = o->ph[i];
       if (v > 0.0) {
-        lo = std::min(lo, log(v));
-        hi = std::max(hi, log(v));
+        pmin = std::min(pmin, v);
+        pmax = std::max(pmax, v);
       }
     }
-    if (!(hi >= lo)) lo = hi = 0.0;
+    double lo = 0.0, hi = 0.0;
+    if (pmax > 0.0) {
+      lo = log(pmin);
+      hi = log(pmax);
+    }
     const double span = std::max(hi - lo, 1e-3) * (1.0 + 1e-6);
     c->lnp_lo = (float)(lo - 1e-6 * span);
     c->lnp_span = span;

@@ -46,7 +46,14 @@ struct lg_ctx {
   // observations
   lg::TypeTable types{};
   lg::ObsDev obs{};
-  std::vector<void*> obs_bufs;
+  // device buffers of the observation set, one slot per upload in the fixed
+  // order lg_set_obs makes them; a slot is reallocated only when a set outgrows it
+  struct ObsSlot {
+    void* p = nullptr;
+    size_t bytes = 0;
+  };
+  std::vector<ObsSlot> obs_slots;
+  size_t obs_slot_next = 0;
   std::vector<int> h_copy_obs, h_copy_block, h_copy_eoff;
   lg::CellIndex cells{};
   bool have_cells = false;
@@ -294,28 +301,46 @@ void drop_graph(lg_ctx* c) {
   for (auto& p : c->graph_key) p = nullptr;
 }
 
+// forget the observation set (its buffers stay allocated for the next one)
 void free_obs(lg_ctx* c) {
-  for (void* p : c->obs_bufs) cudaFree(p);
-  c->obs_bufs.clear();
+  c->obs_slot_next = 0;
   c->obs = lg::ObsDev{};
   c->have_obs = false;
+}
+
+void release_obs_memory(lg_ctx* c) {
+  for (auto& sl : c->obs_slots)
+    if (sl.p) cudaFree(sl.p);
+  c->obs_slots.clear();
+  free_obs(c);
+}
+
+// the next observation buffer of n elements
+template <typename T>
+int scratch(lg_ctx* c, size_t n, T** out) {
+  const size_t bytes = sizeof(T) * std::max<size_t>(n, 1);
+  if (c->obs_slot_next == c->obs_slots.size()) c->obs_slots.push_back({});
+  lg_ctx::ObsSlot& sl = c->obs_slots[c->obs_slot_next++];
+  if (sl.bytes < bytes) {
+    if (sl.p) cudaFree(sl.p);
+    sl.p = nullptr;
+    sl.bytes = 0;
+    const size_t want = bytes + bytes / 4;  // headroom for a somewhat larger next set
+    if (cudaMalloc(&sl.p, want) != cudaSuccess) {
+      cudaGetLastError();
+      return LG_ERR_NOMEM;
+    }
+    sl.bytes = want;
+  }
+  *out = static_cast<T*>(sl.p);
+  return LG_OK;
 }
 
 template <typename T>
 int upload(lg_ctx* c, const T* h, size_t n, const T** out) {
   T* d = nullptr;
-  if (dalloc(&d, n) != LG_OK) return LG_ERR_NOMEM;
-  c->obs_bufs.push_back(d);
+  if (scratch(c, n, &d) != LG_OK) return LG_ERR_NOMEM;
   if (n) CK(cudaMemcpy(d, h, sizeof(T) * n, cudaMemcpyHostToDevice));
-  *out = d;
-  return LG_OK;
-}
-
-template <typename T>
-int scratch(lg_ctx* c, size_t n, T** out) {
-  T* d = nullptr;
-  if (dalloc(&d, n) != LG_OK) return LG_ERR_NOMEM;
-  c->obs_bufs.push_back(d);
   *out = d;
   return LG_OK;
 }
@@ -557,6 +582,8 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
       tt.var[t][v] = ty.var[v];
     }
   }
+  // no analysis of the previous set may still read its buffers
+  CK(cudaDeviceSynchronize());
   free_obs(c);
   c->capacity_ready = false;
   drop_graph(c);
@@ -1775,7 +1802,7 @@ int lg_get_hx(const lg_ctx* c, double* yb, double* dis) {
 void lg_destroy(lg_ctx* c) {
   if (!c) return;
   drop_graph(c);
-  free_obs(c);
+  release_obs_memory(c);
   dfree(c->d_glat); dfree(c->d_glon); dfree(c->d_ca); dfree(c->d_cb); dfree(c->d_blk);
   dfree(c->d_lat_block); dfree(c->d_lon_block); dfree(c->d_nb_off); dfree(c->d_nb_blk);
   dfree(c->hx.yb); dfree(c->hx.yb32); dfree(c->hx.dis); dfree(c->hx.lnp); dfree(c->hx.rdiag);

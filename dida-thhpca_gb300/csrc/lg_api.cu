@@ -1701,7 +1701,9 @@ int lg_gmcore_to_da_device(int ens, int num_lat, int num_lon, int nz, int halo,
                            const double* d_ps, const double* d_u_half, const double* d_v_half,
                            const double* d_pt, const double* d_area_subcell,
                            const double* d_area_cell, double* d_xb, void* stream) {
-  if (ens < 1 || num_lat < 1 || num_lon < 1 || nz < 1 || halo < 0 || halo > num_lon) return LG_ERR_ARG;
+  if (ens < 1 || ens > 1024 || num_lat < 1 || num_lat > 65535 || num_lon < 1 || nz < 1 ||
+      halo < 0 || halo > num_lon)
+    return LG_ERR_ARG;
   if (!d_ps || !d_u_half || !d_v_half || !d_pt || !d_area_subcell || !d_area_cell || !d_xb)
     return LG_ERR_ARG;
   CK(lg::launch_gmcore_to_da(ens, num_lat, num_lon, nz, halo, d_ps, d_u_half, d_v_half, d_pt,

@@ -30,7 +30,7 @@ UNITS = {
     "lg_noalloc.cu": [],
     "lg_prepost.cu": [],
     "lg_cube.cu": [],
-    "lg_coupler.cu": ["-fmad=false"],
+    "lg_coupler.cu": [],
 }
 
 

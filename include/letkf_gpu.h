@@ -230,7 +230,9 @@ int lg_obs_from_records(int nz, int nvar, int n_records, const float* lon, const
  *   area_subcell [lat][2], area_cell [lat]  (GMCORE mesh; device arrays)
  * Output xb [lon + 2 halo][lat + 2 halo][1 + 3 nz][ens] (the lg_run layout with
  * rows ps, u, v, pt): u = (u_f(i) + u_f(i-1)) / 2 (periodic),
- * v = 2 (v_f(j-1) area_subcell(1,j) + v_f(j) area_subcell(2,j)) / area_cell(j);
+ * v = 2 (v_f(j-1) area_subcell(1,j) + v_f(j) area_subcell(2,j)) / area_cell(j)
+ * (evaluated with the per-latitude weights 2 area_subcell / area_cell: equal
+ * up to rounding); ens <= 1024;
  * the longitude halo is filled periodically, latitude halo rows are not
  * written.  Enqueued on stream (NULL: the default stream); no synchronisation. */
 int lg_gmcore_to_da_device(int ens, int num_lat, int num_lon, int nz, int halo,

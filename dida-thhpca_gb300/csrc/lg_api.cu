@@ -961,9 +961,11 @@ int prepare_capacity(lg_ctx* c) {
     if (r != LG_OK) return r;
     c->cube_cs = (int)std::min<size_t>((size_t)c->cube_ns,
                                        std::max<size_t>(1, budget / ((size_t)k * k * sizeof(double))));
-    lg_ctx::SolveLane& L = c->lane[0];
     // mixed precision: tridiagonal form and rotation log for the FP32 trans
     const bool eig2 = cube_trans_fp32(c);
+    // two buffer sets: chunks alternate between two streams
+    for (int li = 0; li < 2; ++li) {
+    lg_ctx::SolveLane& L = c->lane[li];
     if (L.cap < (size_t)c->cube_cs || L.rot_n_cap != (eig2 ? (size_t)c->rot_cap : 0)) {
       dfree(L.C); dfree(L.t); dfree(L.tri); dfree(L.lam); dfree(L.rot_cs); dfree(L.rot_i);
       dfree(L.rot_n); dfree(L.ovf_list); dfree(L.ovf_n);
@@ -984,6 +986,7 @@ int prepare_capacity(lg_ctx* c) {
       if (r != LG_OK) return LG_ERR_NOMEM;
       L.cap = cap;
       L.rot_n_cap = eig2 ? (size_t)c->rot_cap : 0;
+    }
     }
     if (c->trans_cap < (size_t)c->cube_ns) {
       dfree(c->d_trans);
@@ -1161,9 +1164,15 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     // Cube solves, on st: per chunk of solves the Gram at each solve's centre
     // column and level (per-solve kernels) and the solve's explicit trans
     // (FP64 eigensolver); then every column from the cubes that cover it.
+    // chunks alternate between st and the side stream, each with its own
+    // buffer set, so the Gram of one runs beside the eigensolve of the other
     const int cs = c->cube_cs, ns = c->cube_ns;
-    lg_ctx::SolveLane& L = c->lane[0];
+    CK(cudaEventRecord(c->ev_fork, st));
+    CK(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
+    const cudaStream_t st0 = st;
     for (int q = 0; q * cs < ns; ++q) {
+      lg_ctx::SolveLane& L = c->lane[q & 1];
+      const cudaStream_t st = (q & 1) ? c->side_stream : st0;  // this chunk's stream
       cudaEvent_t* kv = &c->kev[7 * q];
       lg::SolveBatch b{};
       b.mode = 0;
@@ -1204,6 +1213,8 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
         launches += 2;
       }
     }
+    CK(cudaEventRecord(c->ev_join, c->side_stream));
+    CK(cudaStreamWaitEvent(st, c->ev_join, 0));
     const lg::CubeDev cd{g.cube_n, g.cube_nz, g.cube_n - g.overlap, c->cube_ngroups,
                          (g.vert_dist > 0.0 && g.overlap == 0) ? 1 : 0, c->d_cube_off};
     lg::launch_cube_apply(geo, cd, c->d_trans, xb, axb, xa, axa, st);

@@ -120,6 +120,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+def job_rate(ms_local, ncol, world, device=None):
+    """Whole-job columns/s of N replicas: the slowest rank's step time (max
+    over ranks when a process group is up) and every rank's columns."""
+    import torch
+    ms = ms_local
+    if world > 1:
+        import torch.distributed as tdist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * ncol / (ms * 1e-3)
+
+
 def measured_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -280,11 +293,7 @@ def main():
     torch.cuda.synchronize()
     clocks = sampler.stop()
     ms = e0.elapsed_time(e1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * ncol / (ms * 1e-3)
+    ms, value = job_rate(ms, ncol, world, dev)
     st = ctx.stats()
 
     # Per-kernel durations without overlap: one more analysis on a single solve

@@ -138,3 +138,31 @@ def test_host_run_pinned_overlapped_copies_match_pageable(mb1, monkeypatch):
         h = cfg.halo
         assert np.all(pxa[:h] == 7.0) and np.all(paxa[:, :h] == 7.0)
         ctx.letkf_final()
+
+
+def test_observation_sets_of_changing_size_reuse_buffers():
+    """One context through a small, a larger and the small observation set
+    again (buffers kept across sets, grown when outgrown) gives the same
+    analyses as fresh contexts."""
+    import letkf_gb300 as lg
+    import synth
+    small = lg.preset("tiny3d")
+    big = small.replace(n_obs=3 * small.n_obs, seed=5)
+    ws, wb = synth.make_workload(small), synth.make_workload(big)
+
+    def fresh(cfg, w):
+        c = lg.Letkf(cfg)
+        c.set_obs(w.obs)
+        xa, axa = np.zeros_like(w.xb), np.zeros_like(w.axb)
+        c.letkf_run(0, w.xb, w.axb, xa, axa)
+        c.letkf_final()
+        return xa, axa
+
+    ref_s, ref_b = fresh(small, ws), fresh(big, wb)
+    ctx = lg.Letkf(small)
+    for w, ref in ((ws, ref_s), (wb, ref_b), (ws, ref_s)):
+        ctx.set_obs(w.obs)
+        xa, axa = np.zeros_like(w.xb), np.zeros_like(w.axb)
+        ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+        assert np.array_equal(xa, ref[0]) and np.array_equal(axa, ref[1])
+    ctx.letkf_final()

@@ -73,6 +73,80 @@ __device__ inline double rcp_nr(double x) {
 // biased exponent of a double (0 for zero and subnormals, 2047 for inf/NaN)
 __device__ inline int dexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
 
+// Sum of one finite double per lane over the warp, on the integer pipe: each
+// value is aligned at the warp's largest exponent into a signed 128-bit fixed
+// point number (parts below 2^-64 of that exponent's unit truncated), the 32
+// numbers are added exactly through a shuffle tree, and the total is rounded
+// once to nearest-even.  The result is within an ulp of the exact sum --
+// closer than a tree of FP64 additions -- and the FP64 pipe issues nothing.
+// Subnormal inputs count as zero.
+__device__ inline double warp_sum_exact(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const int emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)e);
+  if (emax == 0) return 0.0;
+  unsigned long long hi = 0, lo = 0;
+  if (e != 0) {
+    const unsigned long long m = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = emax - e;
+    if (sh == 0) {
+      hi = m;
+    } else if (sh < 64) {
+      hi = m >> sh;
+      lo = m << (64 - sh);
+    } else if (sh == 64) {
+      lo = m;
+    } else if (sh < 128) {
+      lo = m >> (sh - 64);
+    }
+    if (b >> 63) {  // two's complement
+      lo = ~lo + 1;
+      hi = ~hi + (lo == 0 ? 1 : 0);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    const unsigned long long ls = lo + l2;
+    hi = hi + h2 + (ls < lo ? 1 : 0);
+    lo = ls;
+  }
+  const bool neg = (long long)hi < 0;
+  if (neg) {
+    lo = ~lo + 1;
+    hi = ~hi + (lo == 0 ? 1 : 0);
+  }
+  int p;  // leading one
+  if (hi) {
+    p = 127 - __clzll((long long)hi);
+  } else if (lo) {
+    p = 63 - __clzll((long long)lo);
+  } else {
+    return 0.0;
+  }
+  unsigned long long mant, half = 0, sticky = 0;
+  const int drop = p - 52;
+  if (drop <= 0) {
+    mant = lo << (-drop);
+  } else {
+    mant = drop >= 64 ? hi >> (drop - 64) : (hi << (64 - drop)) | (lo >> drop);
+    const int rb = drop - 1;  // highest dropped bit
+    if (rb >= 64) {
+      half = (hi >> (rb - 64)) & 1;
+      sticky = lo != 0 || (hi & ((1ull << (rb - 64)) - 1)) != 0;
+    } else {
+      half = (lo >> rb) & 1;
+      sticky = rb > 0 && (lo & ((1ull << rb) - 1)) != 0;
+    }
+  }
+  mant += (half && (sticky || (mant & 1))) ? 1 : 0;  // may carry into the exponent
+  // 2^p in units of 2^(emax - 1139): biased exponent p + emax - 116
+  const unsigned long long bits = ((unsigned long long)(p + emax - 116 - 1) << 52) + mant;
+  const double r = __longlong_as_double((long long)bits);
+  return neg ? -r : r;
+}
+
 // u32 = 1 (mixed path): the reflectors are written in FP32 for the FP32 vector
 // kernel, normalised as v = u / sqrt(h) (P = I - v v^T, |v|^2 = 2 whatever the
 // size of h, so a rounding-level row of a low-rank matrix neither overflows nor
@@ -121,11 +195,7 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
   double* H = out + 2 * n;
   double* U = out + 3 * n;
   __syncwarp();
-  auto wsum = [](double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-  };
+  auto wsum = [](double v) { return warp_sum_exact(v); };
   float* U32 = reinterpret_cast<float*>(U);
   float* Act32 = U32 + (size_t)n * (n - 1) / 2;
   bool extreme = false;  // some h outside the FP32 reflector range

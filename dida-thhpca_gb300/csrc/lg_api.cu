@@ -21,6 +21,7 @@
 #include <initializer_list>
 
 #include <algorithm>
+#include <thread>
 #include <vector>
 
 #include "lg_internal.h"
@@ -264,6 +265,33 @@ void neighbour_blocks(const lg_ctx* c, int bx, int by, std::vector<int>& out) {
       out.push_back((nby - 1) * gnx + (tbx - 1));
     }
   }
+}
+
+// Host threads for the observation ingest: one per core, at most 16, and
+// none beyond one per min_per items.  LETKF_GB300_HOST_THREADS sets the count
+// (at most one per item), which the tests use to compare thread counts.
+int host_threads(int64_t n, int64_t min_per) {
+  int hw = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+  if (const char* env = getenv("LETKF_GB300_HOST_THREADS")) {
+    hw = std::max(1, std::min(64, atoi(env)));
+    min_per = 1;
+  }
+  return (int)std::max<int64_t>(1, std::min<int64_t>(hw, n / std::max<int64_t>(1, min_per)));
+}
+
+// fn(t, begin, end) over [0, n) in nt contiguous ascending ranges (range t on
+// thread t); the same (nt, n) always gives the same ranges.
+template <typename F>
+void run_ranges(int nt, int64_t n, F&& fn) {
+  if (nt <= 1) {
+    fn(0, (int64_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(nt - 1);
+  for (int t = 1; t < nt; ++t) th.emplace_back([&fn, t, nt, n] { fn(t, n * t / nt, n * (t + 1) / nt); });
+  fn(0, (int64_t)0, n / nt);
+  for (auto& x : th) x.join();
 }
 
 // %.5f-formatted box bound as the Redis server parses it
@@ -609,37 +637,54 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
     lo_lon[by - 1] = box_bound(GN(c, b.z));
     hi_lon[by - 1] = box_bound(GN(c, b.w + 1));
   }
-  std::vector<int> bt_cnt((size_t)nb * T + 1, 0);
+  // Counting pass on host threads over contiguous observation ranges, each
+  // with its own (block, type) counts; the fill pass gives thread t the slots
+  // after those of threads < t in every (block, type) segment, so that the
+  // copies of a segment ascend by observation as in a serial pass.
+  const size_t nbt = (size_t)nb * T;
+  const int nth = host_threads(n, 1 << 15);
+  std::vector<std::vector<int>> cnt_t(nth, std::vector<int>(nbt, 0));
   std::vector<int> rows_of(n * 2), cols_of(n * 2);
   std::vector<unsigned char> nrow(n), ncolb(n);
-  for (int i = 0; i < n; ++i) {
-    const double la = o->lat[i], lo = o->lon[i];
-    int nr = 0, nc = 0;
-    // blocks are contiguous in latitude: binary search for the first
-    int a = (int)(std::lower_bound(hi_lat.begin(), hi_lat.end(), la) - hi_lat.begin());
-    for (int bx = a; bx < g.global_nx && nr < 2; ++bx) {
-      if (la < lo_lat[bx]) break;
-      if (la <= hi_lat[bx]) rows_of[2 * i + nr++] = bx;
+  run_ranges(nth, n, [&](int t, int64_t i0, int64_t i1) {
+    int* cnt = cnt_t[t].data();
+    for (int i = (int)i0; i < (int)i1; ++i) {
+      const double la = o->lat[i], lo = o->lon[i];
+      int nr = 0, nc = 0;
+      // blocks are contiguous in latitude: binary search for the first
+      int a = (int)(std::lower_bound(hi_lat.begin(), hi_lat.end(), la) - hi_lat.begin());
+      for (int bx = a; bx < g.global_nx && nr < 2; ++bx) {
+        if (la < lo_lat[bx]) break;
+        if (la <= hi_lat[bx]) rows_of[2 * i + nr++] = bx;
+      }
+      int bcol = (int)(std::lower_bound(hi_lon.begin(), hi_lon.end(), lo) - hi_lon.begin());
+      for (int by = bcol; by < g.global_ny && nc < 2; ++by) {
+        if (lo < lo_lon[by]) break;
+        if (lo <= hi_lon[by]) cols_of[2 * i + nc++] = by;
+      }
+      nrow[i] = (unsigned char)nr;
+      ncolb[i] = (unsigned char)nc;
+      for (int r = 0; r < nr; ++r)
+        for (int q = 0; q < nc; ++q)
+          cnt[((size_t)cols_of[2 * i + q] * g.global_nx + rows_of[2 * i + r]) * T + o->type[i]]++;
     }
-    int bcol = (int)(std::lower_bound(hi_lon.begin(), hi_lon.end(), lo) - hi_lon.begin());
-    for (int by = bcol; by < g.global_ny && nc < 2; ++by) {
-      if (lo < lo_lon[by]) break;
-      if (lo <= hi_lon[by]) cols_of[2 * i + nc++] = by;
+  });
+  std::vector<int> bt_off(nbt + 1, 0);
+  for (size_t s = 0; s < nbt; ++s) {
+    int run = bt_off[s];
+    for (int t = 0; t < nth; ++t) {  // counts -> this thread's first slot
+      const int k = cnt_t[t][s];
+      cnt_t[t][s] = run;
+      run += k;
     }
-    nrow[i] = (unsigned char)nr;
-    ncolb[i] = (unsigned char)nc;
-    for (int r = 0; r < nr; ++r)
-      for (int q = 0; q < nc; ++q)
-        bt_cnt[((size_t)cols_of[2 * i + q] * g.global_nx + rows_of[2 * i + r]) * T + o->type[i]]++;
+    bt_off[s + 1] = run;
   }
-  std::vector<int> bt_off((size_t)nb * T + 1, 0);
-  for (size_t s = 0; s < (size_t)nb * T; ++s) bt_off[s + 1] = bt_off[s] + bt_cnt[s];
-  const int64_t ncopies = bt_off[(size_t)nb * T];
+  const int64_t ncopies = bt_off[nbt];
   c->h_copy_obs.assign(ncopies, 0);
   c->h_copy_block.assign(ncopies, 0);
-  {
-    std::vector<int> fill(bt_off.begin(), bt_off.end() - 1);
-    for (int i = 0; i < n; ++i)
+  run_ranges(nth, n, [&](int t, int64_t i0, int64_t i1) {
+    int* fill = cnt_t[t].data();
+    for (int i = (int)i0; i < (int)i1; ++i)
       for (int r = 0; r < nrow[i]; ++r)
         for (int q = 0; q < ncolb[i]; ++q) {
           const int b = cols_of[2 * i + q] * g.global_nx + rows_of[2 * i + r];
@@ -647,7 +692,7 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
           c->h_copy_obs[j] = i;
           c->h_copy_block[j] = b;
         }
-  }
+  });
   c->h_copy_eoff.assign(ncopies + 1, 0);
   int64_t ent = 0;
   for (int64_t j = 0; j < ncopies; ++j) {
@@ -736,37 +781,54 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
     std::vector<int> cell_off(nseg + 1, 0), cell_start, perm(ncopies);
     std::vector<int> rowc(ncopies), colc(ncopies);
     int max_len = 0;
-    for (int sg = 0; sg < nseg; ++sg) {
-      const int j0 = bt_off[sg], j1 = bt_off[sg + 1];
-      max_len = std::max(max_len, j1 - j0);
-      int r0 = ci.nrows, r1 = -1, c0 = ci.ncols, c1 = -1;
-      for (int j = j0; j < j1; ++j) {
-        const int oo = c->h_copy_obs[j];
-        int r = (int)floorf(((float)o->lat[oo] + 90.0f) * ci.inv_cell);
-        int cc = (int)floorf((float)o->lon[oo] * ci.inv_cell);
-        r = std::min(std::max(r, 0), ci.nrows - 1);
-        cc = std::min(std::max(cc, 0), ci.ncols - 1);
-        rowc[j] = r;
-        colc[j] = cc;
-        r0 = std::min(r0, r); r1 = std::max(r1, r);
-        c0 = std::min(c0, cc); c1 = std::max(c1, cc);
+    for (int sg = 0; sg < nseg; ++sg) max_len = std::max(max_len, bt_off[sg + 1] - bt_off[sg]);
+    // segments are independent: cells and boxes, then (after the layout of
+    // cell_start) the per-segment counting sort, each on host threads
+    const int nts = host_threads(nseg, 1);
+    run_ranges(nts, nseg, [&](int, int64_t s0, int64_t s1) {
+      for (int sg = (int)s0; sg < (int)s1; ++sg) {
+        const int j0 = bt_off[sg], j1 = bt_off[sg + 1];
+        int r0 = ci.nrows, r1 = -1, c0 = ci.ncols, c1 = -1;
+        for (int j = j0; j < j1; ++j) {
+          const int oo = c->h_copy_obs[j];
+          int r = (int)floorf(((float)o->lat[oo] + 90.0f) * ci.inv_cell);
+          int cc = (int)floorf((float)o->lon[oo] * ci.inv_cell);
+          r = std::min(std::max(r, 0), ci.nrows - 1);
+          cc = std::min(std::max(cc, 0), ci.ncols - 1);
+          rowc[j] = r;
+          colc[j] = cc;
+          r0 = std::min(r0, r); r1 = std::max(r1, r);
+          c0 = std::min(c0, cc); c1 = std::max(c1, cc);
+        }
+        if (j1 == j0) { r0 = 0; r1 = 0; c0 = 0; c1 = 0; }
+        box[sg] = int4{r0, r1 - r0 + 1, c0, c1 - c0 + 1};
       }
-      if (j1 == j0) { r0 = 0; r1 = 0; c0 = 0; c1 = 0; }
-      const int nr = r1 - r0 + 1, ncl = c1 - c0 + 1;
-      box[sg] = int4{r0, nr, c0, ncl};
-      const size_t base = cell_start.size();
-      cell_off[sg] = (int)base;
-      cell_start.resize(base + (size_t)nr * ncl + 1, 0);
-      int* cs = cell_start.data() + base;
-      for (int j = j0; j < j1; ++j) cs[(rowc[j] - r0) * ncl + (colc[j] - c0) + 1]++;
-      for (int q = 0; q < nr * ncl; ++q) cs[q + 1] += cs[q];
-      std::vector<int> fillp(cs, cs + (size_t)nr * ncl);
-      for (int j = j0; j < j1; ++j) {  // stable: positions ascend within a cell
-        const int cell = (rowc[j] - r0) * ncl + (colc[j] - c0);
-        perm[j0 + fillp[cell]++] = j - j0;
+    });
+    {
+      size_t base = 0;
+      for (int sg = 0; sg < nseg; ++sg) {
+        cell_off[sg] = (int)base;
+        base += (size_t)box[sg].y * box[sg].w + 1;
       }
+      cell_off[nseg] = (int)base;
+      cell_start.assign(base, 0);
     }
-    cell_off[nseg] = (int)cell_start.size();
+    run_ranges(nts, nseg, [&](int, int64_t s0, int64_t s1) {
+      std::vector<int> fillp;
+      for (int sg = (int)s0; sg < (int)s1; ++sg) {
+        const int j0 = bt_off[sg], j1 = bt_off[sg + 1];
+        const int r0 = box[sg].x, c0 = box[sg].z, ncl = box[sg].w;
+        const int ncell = box[sg].y * ncl;
+        int* cs = cell_start.data() + cell_off[sg];
+        for (int j = j0; j < j1; ++j) cs[(rowc[j] - r0) * ncl + (colc[j] - c0) + 1]++;
+        for (int q = 0; q < ncell; ++q) cs[q + 1] += cs[q];
+        fillp.assign(cs, cs + ncell);
+        for (int j = j0; j < j1; ++j) {  // stable: positions ascend within a cell
+          const int cell = (rowc[j] - r0) * ncl + (colc[j] - c0);
+          perm[j0 + fillp[cell]++] = j - j0;
+        }
+      }
+    });
     ci.bitmap_words = std::max(1, (max_len + 31) / 32);
     const int4* d_box = nullptr;
     const int *d_cell_off = nullptr, *d_cell_start = nullptr, *d_perm = nullptr;
@@ -777,9 +839,11 @@ int lg_set_obs(lg_ctx* c, const lg_obs_soa* o) {
     rr |= upload(c, perm.data(), perm.size(), &d_perm);
     // per slot: its observation, then the candidate data gathered on the device
     std::vector<int> slot_obs(ncopies);
-    for (int sg = 0; sg < nseg; ++sg)
-      for (int j = bt_off[sg]; j < bt_off[sg + 1]; ++j)
-        slot_obs[j] = c->h_copy_obs[bt_off[sg] + perm[j]];
+    run_ranges(nts, nseg, [&](int, int64_t s0, int64_t s1) {
+      for (int sg = (int)s0; sg < (int)s1; ++sg)
+        for (int j = bt_off[sg]; j < bt_off[sg + 1]; ++j)
+          slot_obs[j] = c->h_copy_obs[bt_off[sg] + perm[j]];
+    });
     const int* d_slot_obs = nullptr;
     float4* d_cand = nullptr;
     rr |= upload(c, slot_obs.data(), slot_obs.size(), &d_slot_obs);

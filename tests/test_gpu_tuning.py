@@ -166,3 +166,26 @@ def test_observation_sets_of_changing_size_reuse_buffers():
         ctx.letkf_run(0, w.xb, w.axb, xa, axa)
         assert np.array_equal(xa, ref[0]) and np.array_equal(axa, ref[1])
     ctx.letkf_final()
+
+
+def test_observation_ingest_is_independent_of_host_threads(monkeypatch):
+    """lg_set_obs's host passes (block assignment of the observations, cell
+    index of every block segment) on 1 and on 5 host threads give the same
+    copy layout, selection lists and analysis, bit for bit."""
+    import letkf_gb300 as lg
+    import synth
+    cfg = lg.preset("tiny3d").replace(n_obs=2000, seed=11)
+    w = synth.make_workload(cfg)
+    out = []
+    for nt in ("1", "5"):
+        monkeypatch.setenv("LETKF_GB300_HOST_THREADS", nt)
+        c = lg.Letkf(cfg)
+        c.set_obs(w.obs)
+        xa, axa = np.zeros_like(w.xb), np.zeros_like(w.axb)
+        c.letkf_run(0, w.xb, w.axb, xa, axa)
+        out.append((c.copy_layout(), c.lists(), xa, axa))
+        c.letkf_final()
+    (lay1, lst1, xa1, axa1), (lay5, lst5, xa5, axa5) = out
+    assert all(np.array_equal(a, b) for a, b in zip(lay1, lay5))
+    assert all(np.array_equal(a, b) for a, b in zip(lst1, lst5))
+    assert np.array_equal(xa1, xa5) and np.array_equal(axa1, axa5)

@@ -418,7 +418,9 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
         const double ei = EE(i);
         const double f = sn * ei, b = cn * ei;
         const double q2 = f * f + g * g;
-        if (q2 == 0.0) {
+        // q2 == 0 on the bit pattern (off the FP64 pipe): a sum of squares is
+        // never -0, and a NaN is not zero either way
+        if ((__double2hiint(q2) | __double2loint(q2)) == 0) {
           EE(i + 1) = 0.0;
           DD(i + 1) -= p;
           EE(m) = 0.0;

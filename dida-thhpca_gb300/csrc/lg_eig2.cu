@@ -73,6 +73,20 @@ __device__ inline double rcp_nr(double x) {
 // biased exponent of a double (0 for zero and subnormals, 2047 for inf/NaN)
 __device__ inline int dexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
 
+// Scalar tests and exact scalings on the bit pattern, off the FP64 pipe:
+// x == 0.0 (either sign); x >= 0.0 for a non-NaN x (-0 included); -x; x / 2
+// for a normal x with biased exponent >= 2.
+__device__ inline bool is_zero_bits(double x) {
+  return ((__double2hiint(x) & 0x7fffffff) | __double2loint(x)) == 0;
+}
+__device__ inline bool nonneg_bits(double x) { return __double2hiint(x) >= 0 || is_zero_bits(x); }
+__device__ inline double neg_bits(double x) {
+  return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
+}
+__device__ inline double half_bits(double x) {
+  return __hiloint2double(__double2hiint(x) - (1 << 20), __double2loint(x));
+}
+
 // Sum of one finite double per lane over the warp, on the integer pipe: each
 // value is aligned at the warp's largest exponent into a signed 128-bit fixed
 // point number (parts below 2^-64 of that exponent's unit truncated), the 32
@@ -208,13 +222,15 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
       for (int c = lane; c <= l; c += 32) ss = fma(row[c], row[c], ss);
       double h0 = wsum(ss);
       double sc = 1.0;
+      bool scaled = false;
       // outside [2^-900, 2^900] (checked on the exponent bits), and not zero
       const int eh = dexp(h0);
-      if ((eh < 1023 - 900 || eh > 1023 + 900) && h0 != 0.0) {
+      if ((eh < 1023 - 900 || eh > 1023 + 900) && !is_zero_bits(h0)) {
         // extreme magnitudes: scale the row by its 1-norm first (as tred2 does)
         double a1 = 0.0;
         for (int c = lane; c <= l; c += 32) a1 += fabs(row[c]);
         sc = wsum(a1);
+        scaled = true;
         const double inv = 1.0 / sc;
         ss = 0.0;
         for (int c = lane; c <= l; c += 32) {
@@ -225,12 +241,13 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
         h0 = wsum(ss);
         __syncwarp();
       }
-      if (h0 == 0.0) {
+      if (is_zero_bits(h0)) {
         ei = row[l];
       } else {
         const double f = row[l];
-        const double gg = (f >= 0.0) ? -sqrt(h0) : sqrt(h0);
-        ei = sc * gg;
+        const double sq = sqrt(h0);
+        const double gg = nonneg_bits(f) ? neg_bits(sq) : sq;  // -sign(sqrt(h0), f)
+        ei = scaled ? sc * gg : gg;
         h = h0 - f * gg;
         __syncwarp();
         if (lane == 0) row[l] = f - gg;
@@ -286,7 +303,9 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
           }
         }
         __syncwarp();  // q[j] of a split row was written by its group's first lane
-        const double kq = wsum(fs) * (0.5 * inv_h);
+        // h lies in [2^-901, 2^902] (h0 is range-checked or rescaled above and
+        // h0 <= h <= 2 h0), so 1/h is normal and halving it is exact
+        const double kq = wsum(fs) * half_bits(inv_h);
         for (int j = lane; j <= l; j += 32) q[j] = fma(-kq, row[j], q[j]);
         __syncwarp();
         // A -= u q^T + q u^T over the packed rows 0..l, lane t, t+32, ...
@@ -315,7 +334,7 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
     if (u32) {
       const int eh = dexp(h);
       const bool in_range = eh >= 1023 - 200 && eh <= 1023 + 200;
-      extreme |= h != 0.0 && !in_range;
+      extreme |= !is_zero_bits(h) && !in_range;
       const float sv = in_range ? rsqrt_f32_of(h) : 0.0f;
       for (int c = lane; c < i; c += 32) U32[e2::uoff(i) + c] = d2f_bits(row[c]) * sv;
       if (lane == 0) Act32[i] = in_range ? 1.0f : 0.0f;

@@ -94,11 +94,23 @@ __device__ inline double half_bits(double x) {
 // once to nearest-even.  The result is within an ulp of the exact sum --
 // closer than a tree of FP64 additions -- and the FP64 pipe issues nothing.
 // Subnormal inputs count as zero.
-__device__ inline double warp_sum_exact(double v) {
+//
+// kWarp: the sum over the warp; otherwise over aligned groups of f lanes (f a
+// power of two, the same in every lane), each group getting its own sum.  All
+// 32 lanes run the same shuffles either way (no early return in the grouped
+// form, where the groups' exponents differ).
+template <bool kWarp>
+__device__ inline double sum_exact(double v, int f) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
   const int e = (int)((b >> 52) & 0x7ff);
-  const int emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)e);
-  if (emax == 0) return 0.0;
+  int emax;
+  if constexpr (kWarp) {
+    emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)e);
+    if (emax == 0) return 0.0;
+  } else {
+    emax = e;
+    for (int o = f >> 1; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  }
   unsigned long long hi = 0, lo = 0;
   if (e != 0) {
     const unsigned long long m = (b & ((1ull << 52) - 1)) | (1ull << 52);
@@ -118,13 +130,18 @@ __device__ inline double warp_sum_exact(double v) {
       hi = ~hi + (lo == 0 ? 1 : 0);
     }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
+  auto add = [&](int o) {
     const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, hi, o);
     const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o);
     const unsigned long long ls = lo + l2;
     hi = hi + h2 + (ls < lo ? 1 : 0);
     lo = ls;
+  };
+  if constexpr (kWarp) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) add(o);
+  } else {
+    for (int o = f >> 1; o > 0; o >>= 1) add(o);
   }
   const bool neg = (long long)hi < 0;
   if (neg) {
@@ -158,8 +175,11 @@ __device__ inline double warp_sum_exact(double v) {
   // 2^p in units of 2^(emax - 1139): biased exponent p + emax - 116
   const unsigned long long bits = ((unsigned long long)(p + emax - 116 - 1) << 52) + mant;
   const double r = __longlong_as_double((long long)bits);
-  return neg ? -r : r;
+  return neg ? neg_bits(r) : r;
 }
+__device__ inline double warp_sum_exact(double v) { return sum_exact<true>(v, 32); }
+// the sum over this lane's aligned group of f lanes (f = 1, 2, 4, .., 32)
+__device__ inline double group_sum_exact(double v, int f) { return sum_exact<false>(v, f); }
 
 // u32 = 1 (mixed path): the reflectors are written in FP32 for the FP32 vector
 // kernel, normalised as v = u / sqrt(h) (P = I - v v^T, |v|^2 = 2 whatever the
@@ -257,8 +277,9 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
         // first takes the whole row j < 32.  The remaining r rows are split
         // over groups of f lanes (f the largest power of two with r f <= 32),
         // each lane summing a run of ceil(R / f) columns, and the group sums
-        // meet by shuffles: the FP64 pipe then issues about R + ceil(R / f) +
-        // log2 f instructions instead of R per 32 rows.
+        // meet in exact fixed-point sums on the integer pipe: the FP64 pipe
+        // then issues about R + ceil(R / f) instructions instead of R per 32
+        // rows.
         const double inv_h = rcp_nr(h);
         double fs = 0.0;
         const int R = l + 1;
@@ -295,7 +316,7 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
             gj = fma(P[off], row[c], gj);
             tc += c + 1;
           }
-          for (int o = f >> 1; o > 0; o >>= 1) gj += __shfl_xor_sync(0xffffffffu, gj, o);
+          if (f > 1) gj = group_sum_exact(gj, f);  // f is the same in every lane
           const double pj = gj * inv_h;
           if (act && pi == 0) {
             q[j] = pj;

@@ -280,7 +280,8 @@ int host_threads(int64_t n, int64_t min_per) {
 }
 
 // fn(t, begin, end) over [0, n) in nt contiguous ascending ranges (range t on
-// thread t); the same (nt, n) always gives the same ranges.
+// thread t); the same (nt, n) always gives the same ranges.  A range whose
+// thread cannot be started runs on the calling thread.
 template <typename F>
 void run_ranges(int nt, int64_t n, F&& fn) {
   if (nt <= 1) {
@@ -288,8 +289,13 @@ void run_ranges(int nt, int64_t n, F&& fn) {
     return;
   }
   std::vector<std::thread> th;
-  th.reserve(nt - 1);
-  for (int t = 1; t < nt; ++t) th.emplace_back([&fn, t, nt, n] { fn(t, n * t / nt, n * (t + 1) / nt); });
+  int t = 1;
+  try {
+    th.reserve(nt - 1);
+    for (; t < nt; ++t) th.emplace_back([&fn, t, nt, n] { fn(t, n * t / nt, n * (t + 1) / nt); });
+  } catch (...) {
+  }
+  for (int u = t; u < nt; ++u) fn(u, n * u / nt, n * (u + 1) / nt);
   fn(0, (int64_t)0, n / nt);
   for (auto& x : th) x.join();
 }

@@ -91,9 +91,11 @@ __device__ inline double half_bits(double x) {
 // value is aligned at the warp's largest exponent into a signed 128-bit fixed
 // point number (parts below 2^-64 of that exponent's unit truncated), the 32
 // numbers are added exactly through a shuffle tree, and the total is rounded
-// once to nearest-even.  The result is within an ulp of the exact sum --
-// closer than a tree of FP64 additions -- and the FP64 pipe issues nothing.
-// Subnormal inputs count as zero.
+// once to nearest-even.  The result is the correctly rounded sum when the
+// exponents span at most 64 binades; otherwise its error is below 32 units of
+// 2^-116 of the largest term's binade plus the final rounding -- far inside a
+// tree of FP64 additions' bound (about 5 * 2^-53 of the largest term) -- and
+// the FP64 pipe issues nothing.  Subnormal inputs count as zero.
 //
 // kWarp: the sum over the warp; otherwise over aligned groups of f lanes (f a
 // power of two, the same in every lane), each group getting its own sum.  All

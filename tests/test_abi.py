@@ -5,6 +5,8 @@ import ctypes as C
 import os
 import re
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -74,3 +76,14 @@ def test_python_mirror_struct_layout_matches_header(built_lib, tmp_path):
         assert int(got[cname]) == C.sizeof(py), cname
         for fname, _ in py._fields_:
             assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, (cname, fname)
+
+
+def test_context_creation_fails_loudly_without_a_gpu(built_lib):
+    """No host fallback: without a CUDA device, creating a context is an
+    error (LG_ERR_CUDA), not a silent CPU path."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    import letkf_gb300 as lg
+    with pytest.raises(RuntimeError, match="LG_ERR_CUDA"):
+        lg.Letkf(lg.preset("tiny2d"))

@@ -11,9 +11,15 @@ value : columns / (device time of one analysis) with the background already
 e2e   : the same metric through the host-array call a DA driver makes
         (lg_set_obs + lg_run with pinned host buffers: observation ingest and the
         background H2D copy, analysis D2H copy inside the timed region).
+e2e is the median over its steps.
+fp64  : (mixed runs) after the timed mixed analyses, the plain-FP64 GPU path on
+        the same inputs: its time per analysis, the speed-up of the mixed path
+        over it, and the mixed analysis' per-variable increment error against it
+        (relative RMS over every interior point; the bar is 1e-4).
 cpu_baseline / --impl reference : the CPU oracle (C restatement of the
         reference's Fortran hot path; the Fortran itself cannot be built here)
-        on the host cores, over a bounded sample of columns, extrapolated.
+        on the host cores, over a bounded sample of columns spread over every
+        latitude band and longitude sector, extrapolated.
 
 Inputs (3.4 GB background for cfg3) exceed the 129 MB L2, so no flush is done
 between steps.  For --gpus N > 1 (torchrun) every rank analyses its own full
@@ -60,6 +66,10 @@ def parse():
                     help="target CPU time of the bounded oracle sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the plain-FP64 analysis of the same workload (mixed runs only)")
+    ap.add_argument("--fp64-steps", type=int, default=1,
+                    help="timed plain-FP64 analyses after one untimed one")
     ap.add_argument("--tune", default="",
                     help="launch settings before timing, e.g. chunk_mb=2048,solve_streams=2")
     ap.add_argument("--autotune", action="store_true",
@@ -160,10 +170,39 @@ def fp64_peak_tflops(torch, dev):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
-def cpu_sample(cfg, obs, xb, axb, seconds, nthreads):
-    """Oracle timing on a bounded sample: H(x) of every observation, then columns
-    from the equator band until ~seconds elapse; returns columns/s for a full
-    analysis (H(x) + all columns at the sampled rate)."""
+def spread_order(cfg, seed=0, n_bands=12, n_sectors=16):
+    """All grid columns in an order whose every prefix is spread over the
+    globe: rounds of one seeded random column from each of n_bands latitude
+    bands x n_sectors longitude sectors, the cells of a round in random order.
+    Column index c = lon * num_lat + lat (0-based)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    nl, nn = cfg.num_lat, cfg.num_lon
+    lat_b = np.minimum(np.arange(nl) * n_bands // nl, n_bands - 1)
+    lon_s = np.minimum(np.arange(nn) * n_sectors // nn, n_sectors - 1)
+    cells = [[] for _ in range(n_bands * n_sectors)]
+    for lo in range(nn):
+        for la in range(nl):
+            cells[lat_b[la] * n_sectors + lon_s[lo]].append(lo * nl + la)
+    for c in cells:
+        rng.shuffle(c)
+    order = []
+    rnd = 0
+    while True:
+        layer = [c[rnd] for c in cells if rnd < len(c)]
+        if not layer:
+            break
+        rng.shuffle(layer)
+        order.extend(layer)
+        rnd += 1
+    return np.asarray(order, np.int32)
+
+
+def cpu_sample(cfg, obs, xb, axb, seconds, nthreads, seed=0):
+    """Oracle timing on a bounded sample: H(x) of every observation, then
+    columns in a globe-spread order (every latitude band and longitude sector)
+    until ~seconds elapse; returns columns/s for a full analysis (H(x) + all
+    columns at the sampled rate) and the sample's description."""
     import numpy as np
     from oracle import oracle as orc
 
@@ -172,23 +211,61 @@ def cpu_sample(cfg, obs, xb, axb, seconds, nthreads):
     o.hx(xb, axb, nthreads)
     t_hx = time.perf_counter() - t0
     ncol = cfg.num_lat * cfg.num_lon
+    order = spread_order(cfg, seed)
     xa = np.zeros_like(xb)
     axa = np.zeros_like(axb)
-    start = cfg.num_lat // 2 + cfg.num_lat * (cfg.num_lon // 3)
-    done, t_cols, chunk = 0, 0.0, max(1, nthreads)
-    while t_cols < seconds and done < ncol:
-        c0 = (start + done) % ncol
-        c1 = min(ncol, c0 + min(chunk, ncol - done))
+    done, t_cols, chunk = 0, 0.0, max(2 * nthreads, 64)
+    while (t_cols < seconds or done < 64) and done < ncol:
+        cols = order[done:done + chunk]
         t0 = time.perf_counter()
-        o.analysis(xb, axb, xa, axa, c0, c1, nthreads)
+        o.analysis_cols(xb, axb, xa, axa, cols, nthreads)
         t_cols += time.perf_counter() - t0
-        done += c1 - c0
-        chunk = min(4 * chunk, max(nthreads, int(done / max(t_cols, 1e-6) * (seconds - t_cols)) + 1))
+        done += cols.size
+        rate = done / max(t_cols, 1e-6)
+        chunk = int(min(4 * chunk, max(2 * nthreads, rate * (seconds - t_cols))))
+        chunk = max(chunk, 2 * nthreads)
     t_full = t_hx + t_cols * ncol / done
-    return ncol / t_full, {
+    used = order[:done]
+    lats = used % cfg.num_lat
+    lons = used // cfg.num_lat
+    info = {
         "sample": f"H(x) of all {obs.n_obs} obs ({t_hx:.2f} s) + {done} of {ncol} columns "
-                  f"({t_cols:.2f} s), extrapolated to the full analysis",
+                  f"({t_cols:.2f} s; {np.unique(lons).size} longitudes, latitude rows "
+                  f"{int(lats.min()) + 1}..{int(lats.max()) + 1} of {cfg.num_lat}), "
+                  f"extrapolated to the full analysis",
+        "sample_columns": int(done), "sample_seconds": round(t_cols, 3),
+        "hx_seconds": round(t_hx, 3),
         "lapack": "OpenBLAS dgemm/dsyevd" if orc.lapack_loaded() else "built-in loops + Jacobi"}
+    return ncol / t_full, info
+
+
+def increment_rel_rms(cfg, xb, axb, got, ref):
+    """Per-variable relative RMS of the analysis-increment difference between
+    two analyses (torch tensors in the lg_run layout, interior points):
+    rms(inc_got - inc_ref) / rms(inc_ref), inc = xa + axa - (xb + axb).  A
+    non-finite value anywhere makes the variable's entry inf."""
+    import torch
+    h = cfg.halo
+    nlon = xb.shape[0] - 2 * h
+    out = {}
+    r0 = 0
+    for v, lv in zip(cfg.var_names, cfg.var_lev):
+        sl = slice(r0, r0 + lv)
+        num = torch.zeros((), dtype=torch.float64, device=xb.device)
+        den = torch.zeros((), dtype=torch.float64, device=xb.device)
+        finite = True
+        for i0 in range(h, h + nlon, 64):
+            j = slice(i0, min(i0 + 64, h + nlon))
+            bg = xb[j, h:-h, sl] + axb[j, h:-h, sl, None]
+            ig = got[0][j, h:-h, sl] + got[1][j, h:-h, sl, None] - bg
+            io = ref[0][j, h:-h, sl] + ref[1][j, h:-h, sl, None] - bg
+            finite = finite and bool(torch.isfinite(ig).all()) and bool(torch.isfinite(io).all())
+            num += ((ig - io) ** 2).sum()
+            den += (io ** 2).sum()
+        val = float(torch.sqrt(num / den)) if finite and float(den) > 0 else float("inf")
+        out[v] = val
+        r0 += lv
+    return out
 
 
 def reference_arm(args):
@@ -201,15 +278,15 @@ def reference_arm(args):
     if rank != 0:
         return
     cfg = lg.preset(args.config)
-    t0 = time.perf_counter()
     w = synth.make_workload(cfg)
     nthreads = os.cpu_count() or 1
     per_step = max(2.0, 120.0 / max(1, args.steps + args.warmup))
     vals = []
     info = {}
+    xb_h, axb_h = np.ascontiguousarray(w.xb), np.ascontiguousarray(w.axb)
     for i in range(args.warmup + args.steps):
-        v, info = cpu_sample(cfg, w.obs, np.ascontiguousarray(w.xb), np.ascontiguousarray(w.axb),
-                             per_step, nthreads)
+        # each step its own globe-spread sample (seed = step index)
+        v, info = cpu_sample(cfg, w.obs, xb_h, axb_h, per_step, nthreads, seed=i)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
@@ -221,7 +298,11 @@ def reference_arm(args):
         "config": {"workload": f"{cfg.name}: {cfg.num_lon}x{cfg.num_lat}x{cfg.nz}, N={cfg.ens}, "
                                f"{cfg.n_obs} obs, L={cfg.local_dist:g} km"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": info["sample"]},
+                         "sample": info["sample"], "sample_columns": info["sample_columns"],
+                         "sample_seconds": info["sample_seconds"],
+                         "hx_seconds": info["hx_seconds"],
+                         "extrapolated": "columns/s of a full analysis = columns / (H(x) time "
+                                         "+ sample time x columns / sample columns)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "C restatement of the reference's Fortran letkf_run (no Fortran compiler, MPI or "
                 "Redis on this image); " + info["lapack"],
@@ -295,6 +376,11 @@ def main():
     ms = e0.elapsed_time(e1) / args.steps
     ms, value = job_rate(ms, ncol, world, dev)
     st = ctx.stats()
+    mixed = cfg.precision == lg.LG_PREC_MIXED
+    # the timed configuration's analysis, kept for the comparison with plain FP64
+    fp64_arm = mixed and not args.no_fp64 and world == 1
+    if fp64_arm:
+        xa_mixed, axa_mixed = xa.clone(), axa.clone()
 
     # Per-kernel durations without overlap: one more analysis on a single solve
     # stream (outside the timed region) gives every kernel its own event time;
@@ -319,7 +405,6 @@ def main():
     k = cfg.ens
     solves = iso["n_solves"]
     fp64_peak = fp64_peak_tflops(torch, dev)
-    mixed = cfg.precision == lg.LG_PREC_MIXED
     kernels = {
         # symmetric Gram p k (k+1) + Yb^T R^-1 d 2 p k, over the non-zero-weight
         # (entry, level) pairs: the flops the product needs, counting each
@@ -375,6 +460,11 @@ def main():
                    "tuning": {kk: v for kk, v in tuning.items() if kk != "ms"}},
         "clocks": clocks,
         "gpu_launches": acc["n_launches"],
+        "selection": {key: st[key] for key in ("nobsl_total", "nobsl_max", "n_capped", "n_band",
+                                                "n_eig_fail", "n_copies", "n_entries")},
+        "selection_note": "n_band: candidate pairs with |ri - 2| < 1e-12, where a 1-ulp libm "
+                          "difference could flip a list decision; n_eig_fail: eigensolves "
+                          "that hit the QL sweep limit",
         "phases_ms": {n: round(v["ms"], 3) for n, v in kernels.items()},
         "phases_note": "kernel event times of one single-stream analysis (no overlap)",
         "kernels": {n: {kk: v[kk] for kk in ("bound", "achieved_tflops") if kk in v}
@@ -417,8 +507,46 @@ def main():
         h2d = nxb.nbytes + naxb.nbytes + sum(a.nbytes for a in (o.type, o.lat, o.lon, o.ph, o.yo, o.rinv))
         h = cfg.halo
         d2h = (nxa[h:-h, h:-h].nbytes + naxa[h:-h, h:-h].nbytes)
-        line["e2e"] = {"value": ncol / min(ts), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                       "d2h_bytes_per_step": int(d2h)}
+        line["e2e"] = {"value": ncol / statistics.median(ts), "unit": UNIT,
+                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                       "steps": len(ts), "ms_per_step": [round(1e3 * t, 1) for t in ts],
+                       "statistic": "median over the e2e steps"}
+
+    if fp64_arm and rank == 0:
+        # The same workload through the plain-FP64 path (FP64 Gram, FP64
+        # eigensolve and transform): its time per analysis, and the mixed
+        # analysis' per-variable increment error against it over every
+        # interior point.  Outside the mixed timed region.
+        ctx.letkf_final()
+        ctx64 = lg.Letkf(cfg.replace(precision=lg.LG_PREC_FP64))
+        ctx64.set_obs(w.obs)
+        ctx64.letkf_run_device(0, xb, axb, xa, axa, stream.cuda_stream)  # untimed
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.fp64_steps):
+            ctx64.letkf_run_device(0, xb, axb, xa, axa, stream.cuda_stream)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = f0.elapsed_time(f1) / args.fp64_steps
+        st64 = ctx64.stats()
+        errs = increment_rel_rms(cfg, xb, axb, (xa_mixed, axa_mixed), (xa, axa))
+        line["fp64"] = {
+            "ms_per_step": ms64, "steps": args.fp64_steps, "value": ncol / (ms64 * 1e-3),
+            "speedup_vs_fp64": ms64 / ms,
+            "increment_rel_rms": errs,
+            "increment_rel_rms_max": max(errs.values()),
+            "tolerance": 1e-4,
+            "within_tolerance": max(errs.values()) <= 1e-4,
+            "ms_gram": st64["ms_gram"], "ms_total_last": st64["ms_total"],
+            "selection": {key: st64[key] for key in ("nobsl_total", "nobsl_max", "n_band",
+                                                      "n_eig_fail")},
+            "note": "plain FP64 GPU path on the same inputs; increment = xa + axa - (xb + axb), "
+                    "rel RMS of (mixed - FP64) per variable over all interior points",
+        }
+        ctx64.letkf_final()
+        ctx = None
 
     if not args.no_cpu_baseline and rank == 0:
         xb_h = xb.cpu().numpy()
@@ -429,7 +557,8 @@ def main():
                                 "sample": info["sample"] + "; " + info["lapack"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.letkf_final()
+    if ctx is not None:
+        ctx.letkf_final()
     if dist:
         tdist.destroy_process_group()
 

@@ -97,7 +97,7 @@ struct lg_ctx {
   int boff_nb = 0;  // bucket count d_boff was sized for
   // launch shapes and bucket boundaries (lg_set_tuning / lg_autotune)
   lg_tuning tune{1024, LG_GRAM_AUTO, 128, 1, 4, 4, 0, 0.0};
-  // status words: [0] err, [1] eig_fail
+  // status words: [0] err, [1] eig_fail, [2] nobsl_max, [3] n_capped
   int* d_status = nullptr;
   unsigned long long* d_band = nullptr;
   // staging for host-array runs
@@ -142,10 +142,25 @@ namespace {
     }                                                                                \
   } while (0)
 
+// Test hook: LETKF_GB300_ALLOC_LIMIT_MB=m makes every device allocation above
+// m MiB fail as an out-of-memory cudaMalloc would, so that the LG_ERR_NOMEM
+// paths can be exercised on the host side without exhausting a GPU.
+size_t alloc_limit_bytes() {
+  const char* e = getenv("LETKF_GB300_ALLOC_LIMIT_MB");
+  return e ? (size_t)std::max(0, atoi(e)) << 20 : (size_t)-1;
+}
+
+// test hook: LETKF_GB300_QL_ITERS=n caps the QL sweeps per eigenvalue (default 60)
+int ql_iter_limit() {
+  const char* e = getenv("LETKF_GB300_QL_ITERS");
+  return e ? std::max(1, atoi(e)) : 60;
+}
+
 template <typename T>
 int dalloc(T** p, size_t n) {
   *p = nullptr;
   if (n == 0) n = 1;
+  if (sizeof(T) * n > alloc_limit_bytes()) return LG_ERR_NOMEM;
   cudaError_t e = cudaMalloc((void**)p, sizeof(T) * n);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -360,6 +375,7 @@ int scratch(lg_ctx* c, size_t n, T** out) {
     sl.p = nullptr;
     sl.bytes = 0;
     const size_t want = bytes + bytes / 4;  // headroom for a somewhat larger next set
+    if (want > alloc_limit_bytes()) return LG_ERR_NOMEM;
     if (cudaMalloc(&sl.p, want) != cudaSuccess) {
       cudaGetLastError();
       return LG_ERR_NOMEM;
@@ -382,6 +398,7 @@ int upload(lg_ctx* c, const T* h, size_t n, const T** out) {
 int ensure_hx(lg_ctx* c, size_t entries) {
   if (entries <= c->hx_entries_cap && c->hx.yb) return LG_OK;
   dfree(c->hx.yb); dfree(c->hx.yb32); dfree(c->hx.dis); dfree(c->hx.lnp); dfree(c->hx.rdiag);
+  c->hx_entries_cap = 0;  // until every buffer of the new size exists
   const size_t cap = entries + 1;
   const size_t k = (size_t)c->cfg.ens;
   int r = LG_OK;
@@ -511,6 +528,7 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   geo.global_nx = g.global_nx;
   geo.global_ny = g.global_ny;
   geo.nblocks = g.global_nx * g.global_ny;
+  geo.ql_max_iter = ql_iter_limit();
   // decomposition (module_da_parallel.F90:84-87 with pro_info_init's argument roles)
   c->x_sec = g.num_lat / g.global_nx;
   c->x_res = g.num_lat % g.global_nx;
@@ -1189,10 +1207,12 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   CK(record_event(c->ev[4], st));
   // selection: count, scan, fill (the lists' capacity was sized by prepare_capacity)
   const bool cells = c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH");
+  lg::ListDev lcount = c->lists;
+  lcount.col_stats = c->d_status + 2;  // nobsl_max, n_capped
   if (cells)
-    lg::launch_search_cells(geo, c->obs, c->cells, c->lists, 0, c->d_band, st);
+    lg::launch_search_cells(geo, c->obs, c->cells, lcount, 0, c->d_band, st);
   else
-    lg::launch_search(geo, c->obs, c->lists, 0, c->d_band, st);
+    lg::launch_search(geo, c->obs, lcount, 0, c->d_band, st);
   lg::launch_scan_counts(c->lists.cnt, c->lists.off, ncol, c->d_scan_tmp, c->scan_tmp_bytes, st);
   launches += 3;  // count pass + the scan's init and scan kernels
   if (cells)
@@ -1532,11 +1552,16 @@ int run_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, dou
   S.nobsl_total = c->list_total;
   S.n_band = (int64_t)band;
   S.n_eig_fail = status[1];
+  S.nobsl_max = status[2];
+  S.n_capped = status[3];
   if (io) {
     S.ms_h2d = elapsed_ms(c->ev_io[0], c->ev_io[1]);
     S.ms_d2h = elapsed_ms(c->ev_io[2], c->ev_io[3]);
   }
   if (status[0] != 0) return status[0];
+  // some eigensolve hit the sweep limit: the analysis is written (the
+  // reference prints dsyevd's ierr and goes on), the caller is told
+  if (status[1] != 0) return LG_ERR_EIG;
   return LG_OK;
 }
 
@@ -1860,6 +1885,23 @@ int lg_get_lists(const lg_ctx* c, int* counts, int* entries, double* rloc, int64
   return LG_OK;
 }
 
+int lg_get_column_list(const lg_ctx* c, int col, int cap, int* entries, double* rloc,
+                       int* count) {
+  if (!c || !count || col < 0 || cap < 0) return LG_ERR_ARG;
+  if (!c->lists.off) return LG_ERR_STATE;
+  const int ncol = c->cfg.num_lat * c->cfg.num_lon;
+  if (col >= ncol) return LG_ERR_ARG;
+  int n = 0;
+  int64_t off = 0;
+  CK(cudaMemcpy(&n, c->lists.cnt + col, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&off, c->lists.off + col, sizeof(int64_t), cudaMemcpyDeviceToHost));
+  *count = n;
+  const int m = std::min(n, cap);
+  if (entries && m) CK(cudaMemcpy(entries, c->lists.ent + off, sizeof(int) * m, cudaMemcpyDeviceToHost));
+  if (rloc && m) CK(cudaMemcpy(rloc, c->lists.rloc + off, sizeof(double) * m, cudaMemcpyDeviceToHost));
+  return LG_OK;
+}
+
 int lg_copy_layout(const lg_ctx* c, int* copy_obs, int* copy_block, int64_t* copy_entry_off,
                    int64_t* n_copies) {
   if (!c || !n_copies) return LG_ERR_ARG;
@@ -1923,6 +1965,7 @@ int lg_core_batch(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
   geo.ens = ens;
   geo.inflation = inflation;
   geo.vert_dist = -1.0;
+  geo.ql_max_iter = ql_iter_limit();
   lg::SolveBatch b{};
   b.mode = 1;
   b.nsolves = nbatch;
@@ -1981,16 +2024,22 @@ int lg_letkf_core(int nanals, int nobsl, const double* hxens, const float* rdiag
   r |= dalloc(&doff, 1);
   if (r == LG_OK) {
     const int64_t zero = 0;
+    bool ok = true;
     if (p) {
-      cudaMemcpy(dh, hxens, sizeof(double) * p * k, cudaMemcpyHostToDevice);
-      cudaMemcpy(df, rdiaginv, sizeof(float) * p, cudaMemcpyHostToDevice);
-      cudaMemcpy(dd, dep, sizeof(double) * p, cudaMemcpyHostToDevice);
-      cudaMemcpy(dr, rloc, sizeof(double) * p, cudaMemcpyHostToDevice);
+      ok = ok && cudaMemcpy(dh, hxens, sizeof(double) * p * k, cudaMemcpyHostToDevice) == cudaSuccess;
+      ok = ok && cudaMemcpy(df, rdiaginv, sizeof(float) * p, cudaMemcpyHostToDevice) == cudaSuccess;
+      ok = ok && cudaMemcpy(dd, dep, sizeof(double) * p, cudaMemcpyHostToDevice) == cudaSuccess;
+      ok = ok && cudaMemcpy(dr, rloc, sizeof(double) * p, cudaMemcpyHostToDevice) == cudaSuccess;
     }
-    cudaMemcpy(dn, &nobsl, sizeof(int), cudaMemcpyHostToDevice);
-    cudaMemcpy(doff, &zero, sizeof(int64_t), cudaMemcpyHostToDevice);
-    r = lg_core_batch(nanals, 1, dn, doff, dh, df, dd, dr, inflation_factor, LG_PREC_FP64, dt, dw,
-                      nullptr);
+    ok = ok && cudaMemcpy(dn, &nobsl, sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
+    ok = ok && cudaMemcpy(doff, &zero, sizeof(int64_t), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (ok) {
+      r = lg_core_batch(nanals, 1, dn, doff, dh, df, dd, dr, inflation_factor, LG_PREC_FP64, dt,
+                        dw, nullptr);
+    } else {
+      cudaGetLastError();
+      r = LG_ERR_CUDA;
+    }
     if (r == LG_OK || r == LG_ERR_EIG) {
       if (cudaMemcpy(trans, dt, sizeof(double) * k * k, cudaMemcpyDeviceToHost) != cudaSuccess ||
           cudaMemcpy(overline_w, dw, sizeof(double) * k, cudaMemcpyDeviceToHost) != cudaSuccess)

@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(NT) eig_apply_kernel(Geometry g, SolveBatch b,
       B::sync();
       const int m = s_m;
       if (m == l) break;
-      if (++iter > 60) {
+      if (++iter > (g.ql_max_iter > 0 ? g.ql_max_iter : 60)) {
         if (tid == 0) s_fail = 1;
         break;
       }

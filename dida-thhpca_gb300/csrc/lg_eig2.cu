@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
                                                  const double* tri, double* lam, LT* rot_cs,
                                                  unsigned char* rot_i, int* rot_n, int rot_cap,
                                                  int* overflow_list, int* overflow_n,
-                                                 int* eig_fail) {
+                                                 int* eig_fail, int max_iter) {
   const int warps = blockDim.x / 32;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int s = (blockIdx.x * warps + w) * 32 + lane;
@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
       }
       if (l >= n - 1) {
         done = true;
-      } else if (++iter > 60) {
+      } else if (++iter > max_iter) {
         fail = true;
         done = true;
       } else {
@@ -826,7 +826,7 @@ void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, cons
     const int ql_blocks = (ns + 32 * ql_warps - 1) / (32 * ql_warps);
     ql_kernel<LT><<<ql_blocks, 32 * ql_warps, smem_q, stream>>>(
         n, ns, (double)(n - 1) / g.inflation, sqrt(g.inflation), tri, lam, rot_cs, rot_i, rot_n,
-        rot_cap, overflow_list, overflow_n, eig_fail);
+        rot_cap, overflow_list, overflow_n, eig_fail, g.ql_max_iter > 0 ? g.ql_max_iter : 60);
     if (ev_ql) record_event(ev_ql, stream);
   }
   if (phases & kEigVectors) {

@@ -27,6 +27,9 @@ struct Geometry {
   double local_dist, vert_dist, inflation, obs_polar;
   int gc_filter, gc_filter_vertical, max_obs;
   int global_nx, global_ny, nblocks, n_types;
+  // QL sweep limit per eigenvalue (tql2 and dsyevd stop at 30-60 sweeps); 0 = 60.
+  // A small value forces non-convergence (a host-side test of LG_ERR_EIG).
+  int ql_max_iter;
   // device arrays
   const float* glat;     // num_lat+1
   const float* glon;     // num_lon+1
@@ -100,6 +103,9 @@ struct ListDev {
   // the counts of the others stay as they are (zero)
   const int* col_list = nullptr;
   int n_list = 0;
+  // count pass only, optional: [0] = max over columns of the count, [1] += 1
+  // per column truncated at max_obs (lg_stats.nobsl_max, n_capped)
+  int* col_stats = nullptr;
 };
 
 // Per-column entry records grouped by ln p bucket (mixed-precision Gram input).

@@ -2,23 +2,22 @@
 // device allocation.
 //
 // Some callers cannot allocate device memory at the moment they run the core:
-// a model time step that is being captured into a CUDA graph (cudaMalloc is not
-// a capturable operation and its implicit synchronisation would break the
-// capture), a host framework that owns the whole device heap through its own
-// pool and forbids other allocators, or a latency-critical assimilation loop
-// in which cudaMalloc/cudaFree would serialise the device.  For them this entry
-// point keeps its working memory -- the per-solve Gram matrices, projected
-// innovations and the eigensolver status word -- in one file-scope
-// `static __device__` array of fixed size, loaded once with the library and held
-// by every GPU that loads it until the process exits.
+// a host framework (a model coupler, an ML runtime) that owns the whole device
+// heap through its own pool allocator and forbids any other allocator on the
+// device, or a tight assimilation loop in which a cudaMalloc/cudaFree pair per
+// call would synchronise the device and serialise the work around it.  For
+// them this entry point keeps its working memory -- the per-solve Gram
+// matrices, projected innovations and the eigensolver status word -- in one
+// file-scope `static __device__` array of fixed size, loaded with the library
+// and held by every GPU that loads it until the process exits.
 //
 // Limits and rules:
 //   * capacity: kScratchDoubles doubles (8 MiB); a call needs
 //     nbatch * (ens*ens + ens) + 8 of them and is rejected with LG_ERR_SHAPE
 //     beyond that (e.g. at most 252 solves of 64 members per call);
 //   * the device address of the array is looked up once per device, with that
-//     device current, on the first call made on it (cudaGetSymbolAddress); make
-//     that first call before any stream capture;
+//     device current, on the first call made on it (cudaGetSymbolAddress), so
+//     that first call does set-up work; make it before any stream capture;
 //   * every call shares the one array and its contents persist between calls;
 //     the status word is cleared at the start of each call, everything else is
 //     fully rewritten; calls that overlap on the GPU (different streams, or

@@ -104,6 +104,10 @@ __global__ void __launch_bounds__(256) search_kernel(Geometry g, ObsDev ob, List
   if (!fill && lane == 0) {
     l.cnt[col] = (int)(written < cap ? written : cap);
     if (l.capped) l.capped[col] = written >= cap;
+    if (l.col_stats) {
+      atomicMax(&l.col_stats[0], (int)(written < cap ? written : cap));
+      if (written >= cap) atomicAdd(&l.col_stats[1], 1);
+    }
   }
   if (!fill && band) {
 #pragma unroll
@@ -460,6 +464,10 @@ __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob
   if (!fill && lane == 0) {
     l.cnt[col] = (int)(written < cap ? written : cap);
     if (l.capped) l.capped[col] = written >= cap;
+    if (l.col_stats) {
+      atomicMax(&l.col_stats[0], (int)(written < cap ? written : cap));
+      if (written >= cap) atomicAdd(&l.col_stats[1], 1);
+    }
   }
   if (!fill && band) {
 #pragma unroll

@@ -344,6 +344,8 @@ def load_library(path: str = LIB_PATH):
     lib.lg_autotune.argtypes = [C.c_void_p] + [C.c_void_p] * 5 + [P(LgTuning)]
     lib.lg_get_lists.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_double),
                                  P(C.c_int64)]
+    lib.lg_get_column_list.argtypes = [C.c_void_p, C.c_int, C.c_int, P(C.c_int), P(C.c_double),
+                                       P(C.c_int)]
     lib.lg_copy_layout.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int64),
                                    P(C.c_int64)]
     lib.lg_get_hx.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
@@ -508,6 +510,18 @@ class Letkf:
         check(self.lib.lg_get_lists(self.h, _ptr(counts, C.c_int), _ptr(ent, C.c_int),
                                     _ptr(rloc, C.c_double), C.byref(total)), "lg_get_lists")
         return counts, ent[:total.value], rloc[:total.value]
+
+    def column_list(self, col: int):
+        """Neighbour list (entries, weights) of one column of the last analysis."""
+        n = C.c_int()
+        check(self.lib.lg_get_column_list(self.h, col, 0, None, None, C.byref(n)),
+              "lg_get_column_list")
+        ent = np.zeros(max(1, n.value), np.int32)
+        rloc = np.zeros(max(1, n.value), np.float64)
+        check(self.lib.lg_get_column_list(self.h, col, n.value, _ptr(ent, C.c_int),
+                                          _ptr(rloc, C.c_double), C.byref(n)),
+              "lg_get_column_list")
+        return ent[:n.value], rloc[:n.value]
 
     def copy_layout(self):
         n = C.c_int64()

@@ -303,6 +303,13 @@ int lg_autotune(lg_ctx* ctx, const double* d_xb, const double* d_axb, double* d_
  * other columns count 0), and lg_stats.nobsl_total sums over those. */
 int lg_get_lists(const lg_ctx* ctx, int* counts, int* entries, double* rloc, int64_t* total);
 
+/* The neighbour list of one column of the last analysis (as lg_get_lists,
+ * without copying every column's list): *count receives its length and the
+ * first min(count, cap) entries / weights are written (NULL arrays: count
+ * only).  Diagnostic for sampled parity checks; no reference counterpart. */
+int lg_get_column_list(const lg_ctx* ctx, int col, int cap, int* entries, double* rloc,
+                       int* count);
+
 /* Layout of block-observation copies built by lg_set_obs: for each copy j
  * (ordered by block b = (by-1)*global_nx + (bx-1), then type, then observation
  * index), copy_obs[j] = observation index, copy_block[j] = b, and
@@ -327,17 +334,17 @@ int lg_core_batch(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
                   double* d_trans, double* d_wbar, void* stream);
 
 /* lg_core_batch for callers that cannot allocate device memory: no counterpart
- * in the reference.  A step being captured into a CUDA graph, a host framework
- * that owns the device heap through its own pool, or a latency-critical loop
- * that must not be serialised by cudaMalloc/cudaFree cannot let the library
- * allocate its working memory; this entry point keeps it (Gram matrices,
- * projected innovations, status word) in one fixed static device array of
- * 8 MiB instead, so it needs nbatch * (ens*ens + ens) + 8 <= 1048576 doubles
- * (e.g. at most 252 solves of 64 members per call) and returns LG_ERR_SHAPE
- * beyond that.  Same arguments and results as lg_core_batch.  The array's
- * device address is looked up on the first call made on each device, so make
- * that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race and must be serialised by the caller. */
+ * in the reference.  A host framework that owns the whole device heap through
+ * its own pool allocator, or a tight loop in which cudaMalloc/cudaFree per call
+ * would synchronise the device, cannot let the library allocate its working
+ * memory; this entry point keeps it (Gram matrices, projected innovations,
+ * status word) in one fixed static device array of 8 MiB instead, so it needs
+ * nbatch * (ens*ens + ens) + 8 <= 1048576 doubles (e.g. at most 252 solves of
+ * 64 members per call) and returns LG_ERR_SHAPE beyond that.  Same arguments
+ * and results as lg_core_batch.  The array's device address is looked up on
+ * the first call made on each device (set-up work), so make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
 int lg_core_batch_noalloc(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
                           const double* d_hxens, const float* d_rdiaginv, const double* d_dep,
                           const double* d_rloc, double inflation, int precision,

@@ -1188,6 +1188,64 @@ int or_analysis(const or_ctx* c, const double* xb, const double* axb, double* xa
   return status;
 }
 
+/* analysis of the listed global columns (any order, each once) after or_hx:
+ * the per-column path of or_analysis over a sample spread across the globe,
+ * for bounded CPU timings and sampled parity checks (no cubes) */
+int or_analysis_cols(const or_ctx* c, const double* xb, const double* axb, double* xa,
+                     double* axa, const int* cols, int ncols, int nthreads, lg_stats* st_out) {
+  if (!c->hx_done) return LG_ERR_STATE;
+  const lg_config* g = &c->cfg;
+  const int k = g->ens;
+  const int ncol_all = g->num_lat * g->num_lon;
+  if (g->cube_n > 1 || g->overlap > 0 || (g->cube_nz > 1 && g->vert_dist > 0.0))
+    return LG_ERR_UNSUPPORTED;
+  for (int i = 0; i < ncols; ++i)
+    if (cols[i] < 0 || cols[i] >= ncol_all) return LG_ERR_ARG;
+  int status = LG_OK;
+  lg_stats tot;
+  memset(&tot, 0, sizeof tot);
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+#endif
+  {
+    col_ws w;
+    memset(&w, 0, sizeof w);
+    w.iws = (int*)malloc(sizeof(int) * (5 * k + 3));
+    w.trans = (double*)malloc(sizeof(double) * k * k);
+    w.wbar = (double*)malloc(sizeof(double) * k);
+    w.alnp = (double*)malloc(sizeof(double) * (g->nz + 1));
+    w.xcol = (double*)malloc(sizeof(double) * k);
+    lg_stats st;
+    memset(&st, 0, sizeof st);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+    for (int i = 0; i < ncols; ++i) {
+      int s = analyse_column(c, cols[i], xb, axb, xa, axa, &w, &st);
+      if (s != LG_OK) status = s;
+    }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+    {
+      tot.n_columns += st.n_columns;
+      tot.n_solves += st.n_solves;
+      tot.nobsl_total += st.nobsl_total;
+      if (st.nobsl_max > tot.nobsl_max) tot.nobsl_max = st.nobsl_max;
+      tot.n_capped += st.n_capped;
+      tot.n_band += st.n_band;
+      tot.n_eig_fail += st.n_eig_fail;
+    }
+    free(w.ent); free(w.rloc_h); free(w.rloc); free(w.rdiag); free(w.dep); free(w.yb); free(w.lnp);
+    free(w.ws); free(w.iws); free(w.trans); free(w.wbar); free(w.alnp); free(w.xcol);
+  }
+  tot.n_copies = c->n_copies;
+  tot.n_entries = c->n_entries;
+  if (st_out) *st_out = tot;
+  return status;
+}
+
 /* run_da_parallel pre-processing (module_da_parallel.F90:186-211): member mean
  * and perturbations of full members xb_in(ens, n, lat, lon) over npts columns;
  * returns LG_ERR_NAN if a NaN is found. */

@@ -57,6 +57,8 @@ def lib(use_lapack: bool = True):
                                  P(C.c_int), P(C.c_int64)]
     L.or_analysis.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), P(C.c_double),
                               P(C.c_double), C.c_int, C.c_int, C.c_int, P(LgStats)]
+    L.or_analysis_cols.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), P(C.c_double),
+                                   P(C.c_double), P(C.c_int), C.c_int, C.c_int, P(LgStats)]
     L.or_column_trans.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
     L.or_core.argtypes = [C.c_int, C.c_int, P(C.c_double), P(C.c_float), P(C.c_double),
                           P(C.c_double), C.c_double, P(C.c_double), P(C.c_double)]
@@ -170,6 +172,37 @@ class Oracle:
         if r != 0:
             raise RuntimeError(f"or_analysis: {r}")
         return st.as_dict()
+
+
+    def analysis_cols(self, xb, axb, xa, axa, cols, nthreads: int = 0):
+        """Analysis of the listed columns only (the others of xa/axa untouched)."""
+        cols = np.ascontiguousarray(cols, np.int32)
+        st = LgStats()
+        r = lib().or_analysis_cols(self.h, _p(xb, C.c_double), _p(axb, C.c_double),
+                                   _p(xa, C.c_double), _p(axa, C.c_double), _p(cols, C.c_int),
+                                   int(cols.size), nthreads, C.byref(st))
+        if r != 0:
+            raise RuntimeError(f"or_analysis_cols: {r}")
+        return st.as_dict()
+
+
+def sample_columns(cfg, n_lat_bands: int, n_lons: int, seed: int = 0):
+    """A column sample spread over the globe: for each of n_lons longitudes
+    (evenly spaced, with a seeded offset) one column in each of n_lat_bands
+    equal latitude bands (a seeded latitude inside the band), plus the two polar
+    rows.  Column index c = (lon - 1) * num_lat + (lat - 1)."""
+    rng = np.random.default_rng(seed)
+    nl, nn = cfg.num_lat, cfg.num_lon
+    lons = (np.arange(n_lons) * nn // n_lons + rng.integers(0, max(1, nn // n_lons))) % nn
+    edges = np.linspace(0, nl, n_lat_bands + 1).astype(int)
+    cols = []
+    for lo in lons:
+        for b in range(n_lat_bands):
+            a, z = edges[b], max(edges[b] + 1, edges[b + 1])
+            cols.append(lo * nl + int(rng.integers(a, z)))
+        cols.append(lo * nl)            # southernmost row
+        cols.append(lo * nl + nl - 1)   # northernmost row
+    return np.unique(np.asarray(cols, np.int32))
 
 
 def core(hxens, rdiaginv, dep, rloc, inflation):

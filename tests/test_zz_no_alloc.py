@@ -1,9 +1,9 @@
 """lg_core_batch_noalloc: the batched letkf_core for callers that cannot
-allocate device memory (inside a CUDA-graph capture, under a host framework
-that owns the device heap, or in a loop where cudaMalloc's synchronisation is
-not acceptable).  It keeps its scratch in a fixed static device array, so two
-calls in a row must give the same results as lg_core_batch, which allocates
-its own scratch, and a batch larger than the array must be refused.
+allocate device memory (a host framework that owns the device heap through its
+own pool, or a loop in which cudaMalloc's synchronisation is not acceptable).
+It keeps its scratch in a fixed static device array, so two calls in a row
+must give the same results as lg_core_batch, which allocates its own scratch,
+and a batch larger than the array must be refused.
 
 This file is collected last so that a failure here leaves every other test
 already run.

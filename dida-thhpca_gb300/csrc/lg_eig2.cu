@@ -275,19 +275,20 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
         if (lane == 0) row[l] = f - gg;
         __syncwarp();
         // p = A u / h over the R = l + 1 rows; element (j, c) is read from row j
-        // for c <= j and from row c (column j) for c > j.  With R > 32, lane j
-        // first takes the whole row j < 32.  The remaining r rows are split
-        // over groups of f lanes (f the largest power of two with r f <= 32),
-        // each lane summing a run of ceil(R / f) columns, and the group sums
-        // meet in exact fixed-point sums on the integer pipe: the FP64 pipe
-        // then issues about R + ceil(R / f) instructions instead of R per 32
-        // rows.
+        // for c <= j and from row c (column j) for c > j.  With R > 32, lanes
+        // first take whole rows, one each, in rounds of 32 (rows 0 .. nfull - 1,
+        // nfull the largest multiple of 32 below R).  The remaining r rows
+        // (1..32) are split over groups of f lanes (f the largest power of two
+        // with r f <= 32), each lane summing a run of ceil(R / f) columns, and
+        // the group sums meet in exact fixed-point sums on the integer pipe:
+        // the FP64 pipe then issues about R + ceil(R / f) instructions instead
+        // of R per 32 rows.
         const double inv_h = rcp_nr(h);
         double fs = 0.0;
         const int R = l + 1;
-        const int nfull = R > 32 ? 32 : 0;
-        if (nfull) {
-          const int j = lane;
+        const int nfull = R > 32 ? ((R - 1) / 32) * 32 : 0;
+        for (int j0 = 0; j0 < nfull; j0 += 32) {
+          const int j = j0 + lane;
           const int tj = tri_idx(j);
           double gj = 0.0;
           int tc = 0;  // c(c+1)/2

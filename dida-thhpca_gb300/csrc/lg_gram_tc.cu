@@ -295,7 +295,8 @@ __global__ void __launch_bounds__(tc::kThreads) gram_tc_kernel(Geometry g, HxDev
   if (b.work && tid == 0) atomicAdd(b.work, (unsigned long long)nproc);
 }
 
-bool gram_tc_supported(int ens) { return ens <= 64; }
+// a tensor-core Gram exists for every ensemble size the library accepts
+bool gram_tc_supported(int ens) { return ens <= 128; }
 
 void launch_gram_tc(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
                     const double* axb, double* C, double* t, int* err, cudaStream_t stream,
@@ -304,6 +305,10 @@ void launch_gram_tc(const Geometry& g, const HxDev& hx, const ListDev& l, const 
   const size_t smem = 2 * tc::kStageBytes + 1024;
   RecDev r{};
   if (rec) r = *rec;
+  if (gram_tc128_supported(g.ens)) {
+    launch_gram_tc128(g, hx, l, b, axb, C, t, err, r, stream);
+    return;
+  }
   cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   gram_tc_kernel<<<b.nsolves, tc::kThreads, smem, stream>>>(g, hx, l, b, axb, C, t, err, r);
 }
@@ -540,6 +545,10 @@ void launch_gram_tc_stream(const Geometry& g, const HxDev& hx, const ListDev& l,
                            const SolveBatch& b, const double* axb, double* C, double* t, int* err,
                            const RecDev& rec, cudaStream_t stream) {
   if (b.nsolves == 0) return;
+  if (gram_tc128_supported(g.ens)) {
+    launch_gram_tc128(g, hx, l, b, axb, C, t, err, rec, stream);
+    return;
+  }
   const size_t smem = 2 * tc::kStageBytes + 1024;
   cudaFuncSetAttribute(gram_tc_stream_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem);

@@ -188,6 +188,12 @@ inline cudaError_t record_event(cudaEvent_t e, cudaStream_t st) {
              : cudaEventRecord(e, st);
 }
 bool gram_col_supported(int ens);
+// 65..128 members: per-solve tcgen05 Gram (analysis records or a core batch);
+// launch_gram_tc and launch_gram_tc_stream route these sizes to it
+bool gram_tc128_supported(int ens);
+void launch_gram_tc128(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
+                       const double* axb, double* C, double* t, int* err, const RecDev& rec,
+                       cudaStream_t stream);
 void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
                      const double* axb, double* C, double* t, int* err, const RecDev& rec,
                      bool lean, int ctas, cudaStream_t stream);

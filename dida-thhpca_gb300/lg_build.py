@@ -25,6 +25,7 @@ UNITS = {
     "lg_gram.cu": [],
     "lg_eig.cu": [],
     "lg_gram_tc.cu": [],
+    "lg_gram_tc128.cu": [],
     "lg_gram_col.cu": [],
     "lg_eig2.cu": [],
     "lg_noalloc.cu": [],

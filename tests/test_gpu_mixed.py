@@ -43,7 +43,7 @@ def test_core_batch_mixed_close_to_fp64():
     import torch
 
     rng = np.random.default_rng(7)
-    for k, p in [(16, 0), (16, 5), (40, 300), (64, 2000)]:
+    for k, p in [(16, 0), (16, 5), (40, 300), (64, 2000), (100, 700), (128, 0), (128, 3000)]:
         hx = rng.standard_normal((p, k))
         hx -= hx.mean(axis=1, keepdims=True)
         rd = (1.0 / rng.uniform(0.5, 2.0, p) ** 2).astype(np.float32)
@@ -97,6 +97,61 @@ def test_mixed_analysis_increment_within_1e4(name, over):
     e_o, _ = o.column_list(5)
     off = np.concatenate([[0], np.cumsum(counts)])
     assert np.array_equal(ent[off[5]:off[6]], e_o)
+    ctx.letkf_final()
+
+
+def _increment_rel_rms_cols(cfg, w, got, ref, cols):
+    """increment_rel_rms restricted to the listed columns."""
+    h = cfg.halo
+    lon = cols // cfg.num_lat + h
+    lat = cols % cfg.num_lat + h
+    xa, axa = got
+    xa_o, axa_o = ref
+    g = xa[lon, lat] + axa[lon, lat][..., None]
+    o = xa_o[lon, lat] + axa_o[lon, lat][..., None]
+    bg = w.xb[lon, lat] + w.axb[lon, lat][..., None]
+    if not np.all(np.isfinite(g)):
+        return {v: float("inf") for v in cfg.var_names}
+    out, r0 = {}, 0
+    for v, lv in zip(cfg.var_names, cfg.var_lev):
+        sl = slice(r0, r0 + lv)
+        d = (g - bg)[:, sl] - (o - bg)[:, sl]
+        out[v] = float(np.sqrt(np.mean(d ** 2)) / np.sqrt(np.mean((o - bg)[:, sl] ** 2)))
+        r0 += lv
+    return out
+
+
+@pytest.mark.parametrize("name", ["tiny3d", "small3d"])
+def test_mixed_128_members_on_tensor_cores_within_1e4(name):
+    """N = 128 (the large-cycle ensemble size) in mixed precision: the Gram runs
+    on the tcgen05 kernel for 65..128 members (Gram work counted, no FP64
+    Gram), and the increment meets the 1e-4 bar against the FP64 oracle --
+    tiny3d over the whole globe, small3d over every 7th column."""
+    import letkf_gb300 as lg
+    import synth
+    from oracle import oracle as orc
+
+    cfg = lg.preset(name).replace(precision=lg.LG_PREC_MIXED, ens=128)
+    w = synth.make_workload(cfg)
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    xa = np.zeros_like(w.xb)
+    axa = np.zeros_like(w.axb)
+    ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+    st = ctx.stats()
+    assert st["n_gram_entries"] > 0 and st["n_eig_fail"] == 0
+    o = orc.Oracle(cfg, w.obs)
+    o.hx(w.xb, w.axb)
+    xa_o = np.zeros_like(w.xb)
+    axa_o = np.zeros_like(w.axb)
+    if name == "tiny3d":
+        o.analysis(w.xb, w.axb, xa_o, axa_o)
+        errs = increment_rel_rms(cfg, w, (xa, axa), (xa_o, axa_o))
+    else:
+        cols = np.arange(0, cfg.num_lat * cfg.num_lon, 7, dtype=np.int32)
+        o.analysis_cols(w.xb, w.axb, xa_o, axa_o, cols)
+        errs = _increment_rel_rms_cols(cfg, w, (xa, axa), (xa_o, axa_o), cols)
+    assert max(errs.values()) <= TOL_INCREMENT, errs
     ctx.letkf_final()
 
 

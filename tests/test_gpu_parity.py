@@ -75,6 +75,23 @@ def test_analysis_matches_oracle(name):
     ctx.letkf_final()
 
 
+@pytest.mark.parametrize("ens", [96, 128])
+def test_analysis_matches_oracle_above_64_members(ens):
+    """The analysis path's eigensolve (warp-per-matrix tridiagonalisation whose
+    matrix-vector product takes whole rows in rounds of 32 lanes, lane-per-matrix
+    QL) at ensemble sizes above 64, FP64, against the oracle."""
+    cfg, w, ctx, o, got, ref = _run_both("tiny3d", ens=ens)
+    counts, ent, _ = ctx.lists()
+    off = np.concatenate([[0], np.cumsum(counts)])
+    for col in range(0, cfg.num_lat * cfg.num_lon, 5):
+        e_o, _ = o.column_list(col)
+        assert np.array_equal(ent[off[col]:off[col + 1]], e_o)
+    assert ctx.stats()["n_eig_fail"] == 0
+    err = _rel_err(cfg, w, got, ref[:2])
+    assert err < RTOL_ANALYSIS, f"ens={ens}: analysis rel err {err:.3e}"
+    ctx.letkf_final()
+
+
 def test_max_obs_cap_truncates_like_reference():
     cfg, w, ctx, o, got, ref = _run_both("small3d", max_obs=40)
     counts, ent, _ = ctx.lists()

@@ -22,9 +22,11 @@ cpu_baseline / --impl reference : the CPU oracle (C restatement of the
         latitude band and longitude sector, extrapolated.
 
 Inputs (3.4 GB background for cfg3) exceed the 129 MB L2, so no flush is done
-between steps.  For --gpus N > 1 (torchrun) every rank analyses its own full
-replica of the workload ("replicas only": the single-GPU analysis holds the
-whole globe); value is the sum of columns over ranks / max step time.
+between steps.  For --gpus N > 1 (torchrun) the globe is column-sharded: rank
+r analyses the columns of its range of longitude blocks (shard.py), each step
+one all-gather of the shards' H(x) rows over NCCL (the observation exchange);
+value is the globe's columns / the slowest rank's step time (strong scaling:
+the total work is fixed).
 """
 import argparse
 import json
@@ -70,6 +72,12 @@ def parse():
                     help="skip the plain-FP64 analysis of the same workload (mixed runs only)")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="timed plain-FP64 analyses after one untimed one")
+    ap.add_argument("--list-gb", type=float, default=64.0,
+                    help="device memory for neighbour lists; above it the globe is analysed "
+                         "in column windows")
+    ap.add_argument("--fresh-background", action="store_true",
+                    help="a fresh seeded perturbation ensemble before every step (default "
+                         "for cfg5, the ten-analysis cycle)")
     ap.add_argument("--tune", default="",
                     help="launch settings before timing, e.g. chunk_mb=2048,solve_streams=2")
     ap.add_argument("--autotune", action="store_true",
@@ -130,9 +138,9 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def job_rate(ms_local, ncol, world, device=None):
-    """Whole-job columns/s of N replicas: the slowest rank's step time (max
-    over ranks when a process group is up) and every rank's columns."""
+def job_rate(ms_local, ncol_total, world, device=None):
+    """Whole-job columns/s: the columns all ranks analysed together over the
+    slowest rank's step time (max over ranks when a process group is up)."""
     import torch
     ms = ms_local
     if world > 1:
@@ -140,7 +148,7 @@ def job_rate(ms_local, ncol, world, device=None):
         t = torch.tensor([ms], dtype=torch.float64, device=device)
         tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
         ms = float(t.item())
-    return ms, world * ncol / (ms * 1e-3)
+    return ms, ncol_total / (ms * 1e-3)
 
 
 def measured_peaks():
@@ -239,14 +247,15 @@ def cpu_sample(cfg, obs, xb, axb, seconds, nthreads, seed=0):
     return ncol / t_full, info
 
 
-def increment_rel_rms(cfg, xb, axb, got, ref):
+def increment_rel_rms(cfg, xb, axb, got, ref, lons=None):
     """Per-variable relative RMS of the analysis-increment difference between
-    two analyses (torch tensors in the lg_run layout, interior points):
-    rms(inc_got - inc_ref) / rms(inc_ref), inc = xa + axa - (xb + axb).  A
-    non-finite value anywhere makes the variable's entry inf."""
+    two analyses (torch tensors in the lg_run layout, interior points, or the
+    interior longitudes [lons[0], lons[1]) only): rms(inc_got - inc_ref) /
+    rms(inc_ref), inc = xa + axa - (xb + axb).  A non-finite value anywhere
+    makes the variable's entry inf."""
     import torch
     h = cfg.halo
-    nlon = xb.shape[0] - 2 * h
+    lon0, lon1 = lons if lons else (0, xb.shape[0] - 2 * h)
     out = {}
     r0 = 0
     for v, lv in zip(cfg.var_names, cfg.var_lev):
@@ -254,8 +263,8 @@ def increment_rel_rms(cfg, xb, axb, got, ref):
         num = torch.zeros((), dtype=torch.float64, device=xb.device)
         den = torch.zeros((), dtype=torch.float64, device=xb.device)
         finite = True
-        for i0 in range(h, h + nlon, 64):
-            j = slice(i0, min(i0 + 64, h + nlon))
+        for i0 in range(h + lon0, h + lon1, 64):
+            j = slice(i0, min(i0 + 64, h + lon1))
             bg = xb[j, h:-h, sl] + axb[j, h:-h, sl, None]
             ig = got[0][j, h:-h, sl] + got[1][j, h:-h, sl, None] - bg
             io = ref[0][j, h:-h, sl] + ref[1][j, h:-h, sl, None] - bg
@@ -310,6 +319,29 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def rotate_perturbations(xb, seed):
+    """A fresh perturbation ensemble from the current one: X <- X Q with Q a
+    seeded random orthogonal matrix acting on the space orthogonal to the
+    member-mean vector (Q 1 = 1).  The members stay zero-mean and their sample
+    covariance is unchanged; every member becomes a new combination of the
+    old ones.  In place, in slabs of longitudes (xb: lon, lat, rows, k)."""
+    import numpy as np
+    import torch
+    k = xb.shape[-1]
+    rng = np.random.default_rng(seed)
+    g, _ = np.linalg.qr(rng.standard_normal((k - 1, k - 1)))
+    # orthonormal basis of the complement of the ones vector (Helmert rows)
+    basis = np.zeros((k, k - 1))
+    for j in range(1, k):
+        basis[:j, j - 1] = 1.0 / np.sqrt(j * (j + 1))
+        basis[j, j - 1] = -j / np.sqrt(j * (j + 1))
+    q = basis @ g @ basis.T + np.full((k, k), 1.0 / k)
+    qt = torch.as_tensor(q, dtype=xb.dtype, device=xb.device)
+    for i0 in range(0, xb.shape[0], 32):
+        sl = xb[i0:i0 + 32]
+        sl.copy_(torch.matmul(sl, qt))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -349,9 +381,46 @@ def main():
     if args.autotune:
         ctx.autotune(xb, axb, xa, axa, stream.cuda_stream)
     tuning = ctx.tuning()
+    if dist:
+        import shard
+        by_range = shard.lon_block_ranges(cfg.global_ny, world)[rank]
+        ctx.set_shard(*by_range)
+        shard_cols = shard.shard_columns(cfg, by_range)
+    # column windows when the whole globe's neighbour lists (12 bytes an entry,
+    # 28 with the mixed path's Gram records) exceed the list budget
+    mixed = cfg.precision == lg.LG_PREC_MIXED
+    bytes_per_entry = 28 if mixed else 12
+    windows = [(0, ncol)]
+    if not dist:
+        counts = ctx.list_counts()
+        if int(counts.sum()) * bytes_per_entry > args.list_gb * 2 ** 30:
+            windows = ctx.windows(int(args.list_gb * 2 ** 30 / bytes_per_entry))
+    fresh = args.fresh_background or args.config == "cfg5"
+    win_ms = [0.0] * len(windows)
 
     def step():
-        ctx.letkf_run_device(0, xb, axb, xa, axa, stream.cuda_stream)
+        """One analysis of the globe; returns the summed stats of its calls."""
+        if dist:
+            shard.sharded_step(ctx, xb, axb, xa, axa, stream.cuda_stream)
+            return ctx.stats()
+        if len(windows) == 1:
+            ctx.letkf_run_device(0, xb, axb, xa, axa, stream.cuda_stream)
+            return ctx.stats()
+        tot = None
+        for wi, (a, b) in enumerate(windows):
+            ctx.set_columns(a, b)
+            ctx.letkf_run_device(0, xb, axb, xa, axa, stream.cuda_stream)
+            st_w = ctx.stats()
+            win_ms[wi] = st_w["ms_total"]
+            if tot is None:
+                tot = dict(st_w)
+            else:
+                for key, v in st_w.items():
+                    if key == "nobsl_max":
+                        tot[key] = max(tot[key], v)
+                    elif key not in ("n_copies", "n_entries"):
+                        tot[key] += v
+        return tot
 
     for _ in range(args.warmup):
         step()
@@ -364,19 +433,32 @@ def main():
     e1 = torch.cuda.Event(enable_timing=True)
     acc = {"ms_gram": 0.0, "ms_eig": 0.0, "ms_hx": 0.0, "ms_search": 0.0, "ms_tridiag": 0.0,
            "ms_ql": 0.0, "ms_vec": 0.0, "n_launches": 0, "n_gram_entries": 0, "n_chunks": 0}
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-        st = ctx.stats()
-        for key in acc:
-            acc[key] += st[key]
-    e1.record(stream)
-    torch.cuda.synchronize()
+    step_ms = []
+    if fresh:
+        # each step on a fresh seeded perturbation ensemble, drawn (untimed)
+        # before the step's own events
+        for i in range(args.steps):
+            rotate_perturbations(xb, 1000 + i)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            st = step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            for key in acc:
+                acc[key] += st[key]
+        ms = sum(step_ms) / args.steps
+    else:
+        e0.record(stream)
+        for _ in range(args.steps):
+            st = step()
+            for key in acc:
+                acc[key] += st[key]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1) / args.steps
     ms, value = job_rate(ms, ncol, world, dev)
-    st = ctx.stats()
-    mixed = cfg.precision == lg.LG_PREC_MIXED
     # the timed configuration's analysis, kept for the comparison with plain FP64
     fp64_arm = mixed and not args.no_fp64 and world == 1
     if fp64_arm:
@@ -386,14 +468,18 @@ def main():
     # stream (outside the timed region) gives every kernel its own event time;
     # in the timed two-stream configuration the Gram of one chunk runs beside the
     # eigensolve of another, so per-phase stream times overlap.
-    if tuning["solve_streams"] != 1:
-        ctx.set_tuning(solve_streams=1)
-        step()
-    step()
-    torch.cuda.synchronize()
-    iso = ctx.stats()
-    if tuning["solve_streams"] != 1:
-        ctx.set_tuning(solve_streams=tuning["solve_streams"])
+    if len(windows) == 1:
+        if tuning["solve_streams"] != 1:
+            ctx.set_tuning(solve_streams=1)
+            step()
+        iso = step()
+        torch.cuda.synchronize()
+        if tuning["solve_streams"] != 1:
+            ctx.set_tuning(solve_streams=tuning["solve_streams"])
+    else:
+        iso = dict(st)  # the last timed step's per-kernel sums (streams overlapping)
+    if dist:
+        iso["ms_hx"] = 0.0  # H(x) ran in its own call (lg_hx_device) before the exchange
     # the analysis is finite everywhere it writes (interior points)
     h = cfg.halo
     if not (bool(torch.isfinite(xa[h:-h, h:-h]).all()) and bool(torch.isfinite(axa[h:-h, h:-h]).all())):
@@ -442,7 +528,8 @@ def main():
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "strong" if world > 1 else "weak",
         "vs_baseline": None,
         "dtype": "bf16/f32 contractions, f64 eig" if cfg.precision == lg.LG_PREC_MIXED else "f64",
         "data": "synthetic (seeded spherical-harmonic ensemble, %s observations)" % (
@@ -456,7 +543,8 @@ def main():
                    "list_entries_per_step": st["nobsl_total"],
                    "gram_entries_per_step": iso["n_gram_entries"],
                    "l2": "inputs (background 3.4 GB) larger than L2; no flush",
-                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "parallelism": (f"column shards over {world} GPUs (longitude blocks, one "
+                                   f"H(x) all-gather per step)") if world > 1 else "single GPU",
                    "tuning": {kk: v for kk, v in tuning.items() if kk != "ms"}},
         "clocks": clocks,
         "gpu_launches": acc["n_launches"],
@@ -466,15 +554,51 @@ def main():
                           "difference could flip a list decision; n_eig_fail: eigensolves "
                           "that hit the QL sweep limit",
         "phases_ms": {n: round(v["ms"], 3) for n, v in kernels.items()},
-        "phases_note": "kernel event times of one single-stream analysis (no overlap)",
+        "phases_note": ("kernel event times of one single-stream analysis (no overlap)"
+                        if len(windows) == 1 else
+                        "kernel event times summed over the windows of the last timed step "
+                        "(solve streams overlapping)"),
         "kernels": {n: {kk: v[kk] for kk in ("bound", "achieved_tflops") if kk in v}
                     for n, v in kernels.items()},
         "roofline": roofline,
         "fp64_peak_tflops": fp64_peak,
     }
 
+    # end to end, sharded: each rank copies in its own background slab (its
+    # longitudes and their halo) from page-locked host memory, runs the sharded
+    # step and copies its columns of the analysis out
+    if not args.no_e2e and dist:
+        h = cfg.halo
+        lon0, lon1 = shard_cols[0] // cfg.num_lat, shard_cols[1] // cfg.num_lat
+        sl = slice(lon0, lon1 + 2 * h)
+        own = slice(lon0 + h, lon1 + h)
+        hxb = torch.empty(xb[sl].shape, dtype=torch.float64, pin_memory=True)
+        haxb = torch.empty(axb[sl].shape, dtype=torch.float64, pin_memory=True)
+        hxa = torch.empty(xa[own].shape, dtype=torch.float64, pin_memory=True)
+        haxa = torch.empty(axa[own].shape, dtype=torch.float64, pin_memory=True)
+        hxb.copy_(xb[sl])
+        haxb.copy_(axb[sl])
+        ts = []
+        for _ in range(args.e2e_steps):
+            tdist.barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            xb[sl].copy_(hxb, non_blocking=True)
+            axb[sl].copy_(haxb, non_blocking=True)
+            step()
+            hxa.copy_(xa[own], non_blocking=True)
+            haxa.copy_(axa[own], non_blocking=True)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        ms_e, val_e = job_rate(1e3 * statistics.median(ts), ncol, world, dev)
+        line["e2e"] = {"value": val_e, "unit": UNIT,
+                       "h2d_bytes_per_step": int(hxb.nbytes + haxb.nbytes),
+                       "d2h_bytes_per_step": int(hxa.nbytes + haxa.nbytes),
+                       "steps": len(ts), "statistic": "median over the e2e steps, max over ranks",
+                       "per_rank": "bytes of rank 0's slab and columns"}
+
     # end to end through the host-array C ABI call
-    if not args.no_e2e and rank == 0:
+    if not args.no_e2e and rank == 0 and not dist:
         hxb = torch.empty(xb.shape, dtype=torch.float64, pin_memory=True)
         haxb = torch.empty(axb.shape, dtype=torch.float64, pin_memory=True)
         hxa = torch.zeros(xb.shape, dtype=torch.float64, pin_memory=True)
@@ -520,6 +644,12 @@ def main():
         ctx.letkf_final()
         ctx64 = lg.Letkf(cfg.replace(precision=lg.LG_PREC_FP64))
         ctx64.set_obs(w.obs)
+        # with column windows: the middle window only (whole longitudes), and
+        # the mixed path's time of that window in the last timed step
+        wa, wb = windows[len(windows) // 2]
+        lons = (wa // cfg.num_lat, wb // cfg.num_lat)
+        if len(windows) > 1:
+            ctx64.set_columns(wa, wb)
         ctx64.letkf_run_device(0, xb, axb, xa, axa, stream.cuda_stream)  # untimed
         torch.cuda.synchronize()
         f0 = torch.cuda.Event(enable_timing=True)
@@ -531,10 +661,13 @@ def main():
         torch.cuda.synchronize()
         ms64 = f0.elapsed_time(f1) / args.fp64_steps
         st64 = ctx64.stats()
-        errs = increment_rel_rms(cfg, xb, axb, (xa_mixed, axa_mixed), (xa, axa))
+        ms_mixed = ms if len(windows) == 1 else win_ms[len(windows) // 2]
+        errs = increment_rel_rms(cfg, xb, axb, (xa_mixed, axa_mixed), (xa, axa),
+                                 None if len(windows) == 1 else lons)
         line["fp64"] = {
-            "ms_per_step": ms64, "steps": args.fp64_steps, "value": ncol / (ms64 * 1e-3),
-            "speedup_vs_fp64": ms64 / ms,
+            "ms_per_step": ms64, "steps": args.fp64_steps, "value": (wb - wa) / (ms64 * 1e-3),
+            "columns": wb - wa, "mixed_ms_same_columns": ms_mixed,
+            "speedup_vs_fp64": ms64 / ms_mixed,
             "increment_rel_rms": errs,
             "increment_rel_rms_max": max(errs.values()),
             "tolerance": 1e-4,
@@ -542,13 +675,16 @@ def main():
             "ms_gram": st64["ms_gram"], "ms_total_last": st64["ms_total"],
             "selection": {key: st64[key] for key in ("nobsl_total", "nobsl_max", "n_band",
                                                       "n_eig_fail")},
-            "note": "plain FP64 GPU path on the same inputs; increment = xa + axa - (xb + axb), "
-                    "rel RMS of (mixed - FP64) per variable over all interior points",
+            "note": ("plain FP64 GPU path on the same inputs; increment = xa + axa - (xb + axb), "
+                     "rel RMS of (mixed - FP64) per variable over all interior points"
+                     + ("" if len(windows) == 1 else
+                        f" of the window of columns [{wa}, {wb}) (longitudes {lons[0]}.."
+                        f"{lons[1] - 1}); speed-up against the mixed time of that window")),
         }
         ctx64.letkf_final()
         ctx = None
 
-    if not args.no_cpu_baseline and rank == 0:
+    if not args.no_cpu_baseline and rank == 0 and not dist:
         xb_h = xb.cpu().numpy()
         axb_h = axb.cpu().numpy()
         nthreads = os.cpu_count() or 1

@@ -125,9 +125,18 @@ struct lg_ctx {
   double* d_trans = nullptr;
   size_t trans_cap = 0;
   bool use_eig2 = false;
-  cudaGraphExec_t graph_exec = nullptr;
-  const void* graph_key[9] = {};
-  int64_t graph_launches = 0;
+  // analysed columns [col0, col1) (lg_set_columns / lg_set_shard; col1 < 0: all)
+  // and the shard's own longitude blocks [shard_by0, shard_by1) (H(x) of
+  // lg_hx_device: the copies of those blocks; shard_by1 < 0: every block)
+  int col0 = 0, col1 = -1;
+  int shard_by0 = 0, shard_by1 = -1;
+  int* d_window = nullptr;  // the window's columns, the selection's column list
+  size_t window_cap = 0;
+  // captured graphs, one per kind of call: [1] H(x) only (lg_hx_device),
+  // [2] the analysis after H(x) (lg_analyse_device), [3] both (lg_run*)
+  cudaGraphExec_t graph_exec[4] = {};
+  const void* graph_key[4][12] = {};
+  int64_t graph_launches[4] = {};
   bool graph_failed = false;
 };
 
@@ -163,6 +172,8 @@ int dalloc(T** p, size_t n) {
   if (sizeof(T) * n > alloc_limit_bytes()) return LG_ERR_NOMEM;
   cudaError_t e = cudaMalloc((void**)p, sizeof(T) * n);
   if (e != cudaSuccess) {
+    fprintf(stderr, "letkf_gb300: device allocation of %zu bytes failed: %s\n", sizeof(T) * n,
+            cudaGetErrorString(e));
     cudaGetLastError();
     return LG_ERR_NOMEM;
   }
@@ -345,9 +356,11 @@ void release_streams(lg_ctx* c) {
 }
 
 void drop_graph(lg_ctx* c) {
-  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
-  c->graph_exec = nullptr;
-  for (auto& p : c->graph_key) p = nullptr;
+  for (int i = 0; i < 4; ++i) {
+    if (c->graph_exec[i]) cudaGraphExecDestroy(c->graph_exec[i]);
+    c->graph_exec[i] = nullptr;
+    for (auto& p : c->graph_key[i]) p = nullptr;
+  }
 }
 
 // forget the observation set (its buffers stay allocated for the next one)
@@ -410,6 +423,29 @@ int ensure_hx(lg_ctx* c, size_t entries) {
   if (r != LG_OK) return LG_ERR_NOMEM;
   c->hx_entries_cap = cap;
   return LG_OK;
+}
+
+// the analysed column range
+int col_begin(const lg_ctx* c) { return c->col0; }
+int col_end(const lg_ctx* c) {
+  return c->col1 < 0 ? c->cfg.num_lat * c->cfg.num_lon : c->col1;
+}
+bool windowed(const lg_ctx* c) {
+  return col_begin(c) != 0 || col_end(c) != c->cfg.num_lat * c->cfg.num_lon;
+}
+
+// copies [j0, j1) and entries [e0, e1) of the shard's own blocks: blocks
+// b = by * global_nx + bx with by in [shard_by0, shard_by1), contiguous in the
+// copy order (block, then type, then observation index)
+void shard_copies(const lg_ctx* c, int64_t* j0, int64_t* j1, int64_t* e0, int64_t* e1) {
+  const int gnx = c->cfg.global_nx;
+  const int by1 = c->shard_by1 < 0 ? c->cfg.global_ny : c->shard_by1;
+  const int b0 = c->shard_by0 * gnx, b1 = by1 * gnx;
+  const std::vector<int>& cb = c->h_copy_block;
+  *j0 = std::lower_bound(cb.begin(), cb.end(), b0) - cb.begin();
+  *j1 = std::lower_bound(cb.begin(), cb.end(), b1) - cb.begin();
+  *e0 = c->h_copy_eoff.empty() ? 0 : c->h_copy_eoff[*j0];
+  *e1 = c->h_copy_eoff.empty() ? 0 : c->h_copy_eoff[*j1];
 }
 
 }  // namespace
@@ -999,6 +1035,23 @@ int prepare_capacity(lg_ctx* c) {
     // the cube plan first: only the cube centres' lists are built
     const int r = build_cube_plan(c);
     if (r != LG_OK) return r;
+  } else if (windowed(c)) {
+    // a column window: the selection builds the window's lists only
+    const int n = col_end(c) - col_begin(c);
+    if ((size_t)n > c->window_cap) {
+      dfree(c->d_window);
+      c->window_cap = 0;
+      if (dalloc(&c->d_window, (size_t)n) != LG_OK) return LG_ERR_NOMEM;
+      c->window_cap = (size_t)n;
+    }
+    std::vector<int> cols(n);
+    for (int i = 0; i < n; ++i) cols[i] = col_begin(c) + i;
+    CK(cudaMemcpy(c->d_window, cols.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    c->lists.col_list = c->d_window;
+    c->lists.n_list = n;
+  } else {
+    c->lists.col_list = nullptr;
+    c->lists.n_list = 0;
   }
   CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
   if (c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH"))
@@ -1037,7 +1090,8 @@ int prepare_capacity(lg_ctx* c) {
   const size_t per_col = (size_t)levels * k * k * sizeof(double);
   size_t budget = (size_t)c->tune.chunk_mb << 20;
   if (const char* env = getenv("LETKF_GB300_CHUNK_MB")) budget = (size_t)std::max(1, atoi(env)) << 20;
-  c->chunk = (int)std::min<size_t>((size_t)ncol, std::max<size_t>(1, budget / per_col));
+  const int nsel = col_end(c) - col_begin(c);
+  c->chunk = (int)std::min<size_t>((size_t)nsel, std::max<size_t>(1, budget / per_col));
   c->use_eig2 = lg::eig2_supported(geo);
   c->rot_cap = 3 * k * k;
   // test hook: a small log forces the overflow fallback path
@@ -1121,7 +1175,7 @@ int prepare_capacity(lg_ctx* c) {
     L.cap = cap;
     L.rot_n_cap = (size_t)c->rot_cap;
   }
-  const int nchunks = (ncol + c->chunk - 1) / c->chunk;
+  const int nchunks = (nsel + c->chunk - 1) / c->chunk;
   while ((int)c->kev.size() < 7 * nchunks) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
@@ -1170,18 +1224,26 @@ cudaError_t copy_cols_d2h(const lg_config& g, double* dst, const double* src, si
   return cudaSuccess;
 }
 
+// Parts of an analysis: H(x) (of every block copy, or of the shard's own
+// copies), and everything after it (selection and solves of the analysed
+// columns, with the H(x) in the context's buffers).
+enum : int { kPhaseHx = 1, kPhaseAnalysis = 2, kPhaseAll = 3 };
+
 // Every kernel of one analysis, on stream st; no host synchronisation.
 int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, double* axa,
-                     cudaStream_t st, int64_t* launches_out, const HostIO* io = nullptr) {
+                     cudaStream_t st, int64_t* launches_out, const HostIO* io = nullptr,
+                     int phases = kPhaseAll, bool own_copies = false) {
   const lg_config& g = c->cfg;
   const Geometry& geo = c->geo;
   const int ncol = g.num_lat * g.num_lon;
   const int k = g.ens;
   int64_t launches = 0;
   CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * 4, st));
-  CK(cudaMemsetAsync(c->d_band, 0, sizeof(unsigned long long), st));
-  CK(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), st));
-  CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
+  if (phases & kPhaseAnalysis) {
+    CK(cudaMemsetAsync(c->d_band, 0, sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
+  }
   CK(record_event(c->ev[0], st));
   // H(x) on the side stream, beside the selection on st (the selection needs
   // only observation positions; the records and Grams wait for H(x))
@@ -1200,10 +1262,22 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     CK(cudaEventRecord(c->ev_copy_in, c->copy_stream));
     CK(cudaStreamWaitEvent(c->side_stream, c->ev_copy_in, 0));
   }
-  lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, c->side_stream);
-  launches += c->obs.n_copies > 0;
+  if (phases & kPhaseHx) {
+    int64_t j0 = 0, j1 = c->obs.n_copies, e0 = 0, e1 = 0;
+    if (own_copies) shard_copies(c, &j0, &j1, &e0, &e1);
+    lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, c->side_stream, j0, j1);
+    launches += j1 > j0;
+  }
   CK(record_event(c->ev[1], c->side_stream));
   CK(cudaEventRecord(c->ev_hx, c->side_stream));
+  if (!(phases & kPhaseAnalysis)) {
+    // H(x) only: the selection and solve events are empty intervals
+    CK(cudaStreamWaitEvent(st, c->ev_hx, 0));
+    for (int e : {4, 5, 2, 3}) CK(record_event(c->ev[e], st));
+    CK(cudaGetLastError());
+    *launches_out = launches;
+    return LG_OK;
+  }
   CK(record_event(c->ev[4], st));
   // selection: count, scan, fill (the lists' capacity was sized by prepare_capacity)
   const bool cells = c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH");
@@ -1227,8 +1301,8 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   if (mixed_tc) {
     const int nb = c->tune.lnp_buckets;
     const float inv_dz = (float)(nb / c->lnp_span);
-    lg::launch_records(ncol, c->lists, c->hx, c->lnp_lo, inv_dz, nb,
-                       c->d_boff, c->d_rec, st);
+    lg::launch_records(col_begin(c), col_end(c) - col_begin(c), c->lists, c->hx, c->lnp_lo,
+                       inv_dz, nb, c->d_boff, c->d_rec, st);
     launches += 1;
     rec.r = c->d_rec;
     rec.boff = c->d_boff;
@@ -1319,7 +1393,8 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   }
   const int levels = g.vert_dist > 0.0 ? g.nz : 1;
   const int chunk = c->chunk;
-  const int nchunks = (ncol + chunk - 1) / chunk;
+  const int c0w = col_begin(c), c1w = col_end(c);  // the analysed columns
+  const int nchunks = (c1w - c0w + chunk - 1) / chunk;
   // tensor-core Gram variant.  Auto: the lean column Gram beside the phase
   // pipeline's other streams, the full-size one otherwise; per-solve streaming
   // where the column kernel does not apply.
@@ -1372,8 +1447,8 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     cudaEvent_t* kv = &c->kev[7 * q];
     lg::SolveBatch b{};
     b.mode = 0;
-    b.first_col = q * chunk;
-    b.ncols = std::min(chunk, ncol - b.first_col);
+    b.first_col = c0w + q * chunk;
+    b.ncols = std::min(chunk, c1w - b.first_col);
     b.levels = levels;
     b.nsolves = b.ncols * levels;
     b.work = c->d_work;
@@ -1472,9 +1547,10 @@ namespace {
 // One analysis on device arrays; with io, the host copies of lg_run run inside
 // it (see HostIO).
 int run_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, double* axa,
-                 cudaStream_t st, const HostIO* io) {
+                 cudaStream_t st, const HostIO* io, int phases = kPhaseAll,
+                 bool own_copies = false) {
   const lg_config& g = c->cfg;
-  const int ncol = g.num_lat * g.num_lon;
+  const int nsel = col_end(c) - col_begin(c);
   lg_stats& S = c->stats;
   memset(&S, 0, sizeof S);
   int r = prepare_capacity(c);
@@ -1483,39 +1559,46 @@ int run_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, dou
   // The whole analysis is captured once into a CUDA graph per (arrays, stream)
   // and replayed afterwards; LETKF_GB300_NO_GRAPH=1 runs it eagerly.
   const bool graphs = !getenv("LETKF_GB300_NO_GRAPH") && !c->graph_failed;
-  const void* key[9] = {xb, axb, xa, axa, st, io ? io->xb : nullptr, io ? io->axb : nullptr,
-                        io ? io->xa : nullptr, io ? io->axa : nullptr};
+  const void* key[12] = {xb, axb, xa, axa, st, io ? io->xb : nullptr, io ? io->axb : nullptr,
+                         io ? io->xa : nullptr, io ? io->axa : nullptr,
+                         (const void*)(intptr_t)c->col0, (const void*)(intptr_t)c->col1,
+                         (const void*)(intptr_t)(phases | (own_copies ? 4 : 0) |
+                                                 (c->shard_by0 << 3) | ((c->shard_by1 + 1) << 16))};
   bool ran = false;
   if (graphs) {
-    if (c->graph_exec && memcmp(key, c->graph_key, sizeof key) != 0) drop_graph(c);
-    if (!c->graph_exec) {
+    cudaGraphExec_t& gx = c->graph_exec[phases];
+    if (gx && memcmp(key, c->graph_key[phases], sizeof key) != 0) {
+      cudaGraphExecDestroy(gx);
+      gx = nullptr;
+    }
+    if (!gx) {
       cudaGraph_t graph = nullptr;
       bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess;
       int er = LG_OK;
-      if (ok) er = enqueue_analysis(c, xb, axb, xa, axa, st, &launches, io);
+      if (ok) er = enqueue_analysis(c, xb, axb, xa, axa, st, &launches, io, phases, own_copies);
       const cudaError_t ee = ok ? cudaStreamEndCapture(st, &graph) : cudaErrorUnknown;
       ok = ok && er == LG_OK && ee == cudaSuccess && graph != nullptr;
       if (ok)
-        ok = cudaGraphInstantiateWithFlags(&c->graph_exec, graph,
+        ok = cudaGraphInstantiateWithFlags(&gx, graph,
                                            cudaGraphInstantiateFlagUseNodePriority) == cudaSuccess;
       if (graph) cudaGraphDestroy(graph);
       if (!ok) {
         cudaGetLastError();
-        c->graph_exec = nullptr;
+        gx = nullptr;
         c->graph_failed = true;  // keep running eagerly from now on
       } else {
-        memcpy(c->graph_key, key, sizeof key);
-        c->graph_launches = launches;
+        memcpy(c->graph_key[phases], key, sizeof key);
+        c->graph_launches[phases] = launches;
       }
     }
-    if (c->graph_exec) {
-      CK(cudaGraphLaunch(c->graph_exec, st));
-      launches = c->graph_launches;
+    if (gx) {
+      CK(cudaGraphLaunch(gx, st));
+      launches = c->graph_launches[phases];
       ran = true;
     }
   }
   if (!ran) {
-    r = enqueue_analysis(c, xb, axb, xa, axa, st, &launches, io);
+    r = enqueue_analysis(c, xb, axb, xa, axa, st, &launches, io, phases, own_copies);
     if (r != LG_OK) return r;
   }
   int status[4];
@@ -1524,8 +1607,9 @@ int run_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, dou
   CK(cudaMemcpyAsync(&band, c->d_band, sizeof(band), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&work, c->d_work, sizeof(work), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  const int nchunks = c->cubes ? (c->cube_ns + c->cube_cs - 1) / c->cube_cs
-                               : (ncol + c->chunk - 1) / c->chunk;
+  const int nchunks = !(phases & kPhaseAnalysis) ? 0
+                      : c->cubes ? (c->cube_ns + c->cube_cs - 1) / c->cube_cs
+                                 : (nsel + c->chunk - 1) / c->chunk;
   for (int q = 0; q < nchunks; ++q) {
     const cudaEvent_t* kv = &c->kev[7 * q];
     const float a = elapsed_ms(kv[0], kv[1]);
@@ -1545,11 +1629,14 @@ int run_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, dou
   S.ms_total = elapsed_ms(c->ev[0], c->ev[3]);
   S.n_launches = launches;
   S.n_gram_entries = (int64_t)work;
-  S.n_columns = ncol;
-  S.n_solves = c->cubes ? (int64_t)c->cube_ns : (int64_t)ncol * (g.vert_dist > 0.0 ? g.nz : 1);
+  const bool analysed = (phases & kPhaseAnalysis) != 0;
+  S.n_columns = analysed ? nsel : 0;
+  S.n_solves = !analysed ? 0
+               : c->cubes ? (int64_t)c->cube_ns
+                          : (int64_t)nsel * (g.vert_dist > 0.0 ? g.nz : 1);
   S.n_copies = c->obs.n_copies;
   S.n_entries = c->obs.n_entries;
-  S.nobsl_total = c->list_total;
+  S.nobsl_total = analysed ? c->list_total : 0;
   S.n_band = (int64_t)band;
   S.n_eig_fail = status[1];
   S.nobsl_max = status[2];
@@ -1584,6 +1671,120 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   return run_analysis(c, xb, axb, xa, axa, st, nullptr);
 }
 
+int lg_list_counts(lg_ctx* c, int* counts, int64_t* total) {
+  if (!c || !counts) return LG_ERR_ARG;
+  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
+  if (c->cubes) return LG_ERR_UNSUPPORTED;
+  const int ncol = c->cfg.num_lat * c->cfg.num_lon;
+  if (!c->lists.cnt) {
+    int r = LG_OK;
+    r |= dalloc(&c->lists.cnt, ncol + 1);
+    r |= dalloc(&c->lists.off, ncol + 1);
+    r |= dalloc(&c->lists.capped, ncol);
+    c->scan_tmp_bytes = lg::scan_tmp_bytes(ncol);
+    r |= dalloc((char**)&c->d_scan_tmp, c->scan_tmp_bytes);
+    if (r != LG_OK) return LG_ERR_NOMEM;
+  }
+  cudaStream_t st = c->own_stream;
+  lg::ListDev l = c->lists;
+  l.col_list = nullptr;  // every column
+  l.n_list = 0;
+  CK(cudaMemsetAsync(l.cnt, 0, sizeof(int) * (ncol + 1), st));
+  if (c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH"))
+    lg::launch_search_cells(c->geo, c->obs, c->cells, l, 0, nullptr, st);
+  else
+    lg::launch_search(c->geo, c->obs, l, 0, nullptr, st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(counts, l.cnt, sizeof(int) * ncol, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (total) {
+    int64_t t = 0;
+    for (int i = 0; i < ncol; ++i) t += counts[i];
+    *total = t;
+  }
+  c->capacity_ready = false;  // the next analysis recounts its own columns
+  return LG_OK;
+}
+
+int lg_set_columns(lg_ctx* c, int col_begin, int col_end) {
+  if (!c) return LG_ERR_ARG;
+  const int ncol = c->cfg.num_lat * c->cfg.num_lon;
+  if (col_begin < 0 || col_end > ncol || col_begin >= col_end) return LG_ERR_ARG;
+  if (c->cubes && (col_begin != 0 || col_end != ncol)) return LG_ERR_UNSUPPORTED;
+  c->col0 = col_begin;
+  c->col1 = col_end;
+  c->shard_by0 = 0;
+  c->shard_by1 = -1;
+  c->capacity_ready = false;
+  drop_graph(c);
+  return LG_OK;
+}
+
+int lg_set_shard(lg_ctx* c, int lon_block_begin, int lon_block_end) {
+  if (!c) return LG_ERR_ARG;
+  if (!c->have_grid) return LG_ERR_STATE;
+  const lg_config& g = c->cfg;
+  if (lon_block_begin < 0 || lon_block_end > g.global_ny || lon_block_begin >= lon_block_end)
+    return LG_ERR_ARG;
+  // the blocks' longitudes, all latitudes (pro_info_get_indx with bx = 1)
+  int s0, e0, lon_s, lon_e, s1, e1, lon_s2, lon_e2;
+  get_indx(c, 1, lon_block_begin + 1, &s0, &e0, &lon_s, &lon_e);
+  get_indx(c, 1, lon_block_end, &s1, &e1, &lon_s2, &lon_e2);
+  const int r = lg_set_columns(c, (lon_s - 1) * g.num_lat, lon_e2 * g.num_lat);
+  if (r != LG_OK) return r;
+  c->shard_by0 = lon_block_begin;
+  c->shard_by1 = lon_block_end;
+  return LG_OK;
+}
+
+int lg_shard_entries(const lg_ctx* c, int64_t* entry_begin, int64_t* entry_end,
+                     int64_t* n_entries) {
+  if (!c || !entry_begin || !entry_end) return LG_ERR_ARG;
+  if (!c->have_obs) return LG_ERR_STATE;
+  int64_t j0, j1;
+  shard_copies(c, &j0, &j1, entry_begin, entry_end);
+  if (n_entries) *n_entries = c->obs.n_entries;
+  return LG_OK;
+}
+
+int lg_hx_device(lg_ctx* c, const double* xb, const double* axb, void* stream_v) {
+  if (!c || !xb || !axb) return LG_ERR_ARG;
+  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
+  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+  return run_analysis(c, xb, axb, nullptr, nullptr, st, nullptr, kPhaseHx, true);
+}
+
+int lg_analyse_device(lg_ctx* c, const double* xb, const double* axb, double* xa, double* axa,
+                      void* stream_v) {
+  if (!c || !xb || !axb || !xa || !axa) return LG_ERR_ARG;
+  if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
+  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+  return run_analysis(c, xb, axb, xa, axa, st, nullptr, kPhaseAnalysis, false);
+}
+
+int lg_hx_export(const lg_ctx* c, double* d_rows, void* stream_v) {
+  if (!c || !d_rows) return LG_ERR_ARG;
+  if (!c->have_obs) return LG_ERR_STATE;
+  int64_t j0, j1, e0, e1;
+  shard_copies(c, &j0, &j1, &e0, &e1);
+  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+  lg::launch_hx_export(c->cfg.ens, e0, e1, c->hx, d_rows, st);
+  CK(cudaGetLastError());
+  return LG_OK;
+}
+
+int lg_hx_import(lg_ctx* c, const double* d_rows, int64_t entry_begin, int64_t entry_end,
+                 void* stream_v) {
+  if (!c || (!d_rows && entry_end > entry_begin)) return LG_ERR_ARG;
+  if (!c->have_obs) return LG_ERR_STATE;
+  if (entry_begin < 0 || entry_end < entry_begin || entry_end > c->obs.n_entries)
+    return LG_ERR_SHAPE;
+  cudaStream_t st = stream_v ? (cudaStream_t)stream_v : c->own_stream;
+  lg::launch_hx_import(c->cfg.ens, entry_begin, entry_end, c->hx, d_rows, st);
+  CK(cudaGetLastError());
+  return LG_OK;
+}
+
 int lg_run(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* xa, double* axa) {
   if (!c || !xb || !axb || !xa || !axa) return LG_ERR_ARG;
   if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
@@ -1613,17 +1814,11 @@ int lg_run(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* x
   CK(cudaEventRecord(c->ev_io[1], st));
   int r = lg_run_device(c, ntimes, c->d_xb, c->d_axb, c->d_xa, c->d_axa, st);
   if (r != LG_OK) return r;
-  // interior columns only: for each longitude the interior latitudes are contiguous
-  const size_t h = g.halo;
-  const size_t pitch_x = nlat_e * n * k * sizeof(double), pitch_a = nlat_e * n * sizeof(double);
-  const size_t off_x = (h + h * nlat_e) * n * k, off_a = (h + h * nlat_e) * n;
+  // the analysed interior columns only (every interior column unless a window
+  // is set): for each longitude the interior latitudes are contiguous
   CK(cudaEventRecord(c->ev_io[2], st));
-  CK(cudaMemcpy2DAsync(xa + off_x, pitch_x, c->d_xa + off_x, pitch_x,
-                       (size_t)g.num_lat * n * k * sizeof(double), g.num_lon,
-                       cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpy2DAsync(axa + off_a, pitch_a, c->d_axa + off_a, pitch_a,
-                       (size_t)g.num_lat * n * sizeof(double), g.num_lon,
-                       cudaMemcpyDeviceToHost, st));
+  CK(copy_cols_d2h(g, xa, c->d_xa, n * k, col_begin(c), col_end(c), st));
+  CK(copy_cols_d2h(g, axa, c->d_axa, n, col_begin(c), col_end(c), st));
   CK(cudaEventRecord(c->ev_io[3], st));
   CK(cudaStreamSynchronize(st));
   c->stats.ms_h2d = elapsed_ms(c->ev_io[0], c->ev_io[1]);
@@ -1948,6 +2143,7 @@ void lg_destroy(lg_ctx* c) {
   if (c->ev_hx) cudaEventDestroy(c->ev_hx);
   for (auto& e : c->kev) cudaEventDestroy(e);
   dfree(c->d_work);
+  dfree(c->d_window);
   release_streams(c);
   delete c;
 }

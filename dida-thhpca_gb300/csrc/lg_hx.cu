@@ -8,6 +8,8 @@
 // with the reference's operation order and no contraction (this file is built
 // with -fmad=false).  Lanes own members e = lane, lane+32, ...; the member mean
 // is summed sequentially in member order, as the Fortran loop does.
+#include <algorithm>
+
 #include "lg_device.cuh"
 #include "lg_internal.h"
 
@@ -92,9 +94,10 @@ __device__ inline double bilin(const double* xb, const double* axb, int k, int n
 constexpr int kMaxMemberSlots = 4;  // ens <= 128
 
 __global__ void __launch_bounds__(128) hx_kernel(Geometry g, ObsDev ob, const double* xb,
-                                                 const double* axb, HxDev hx, int* err) {
-  const int64_t j = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x / 32);
-  if (j >= ob.n_copies) return;
+                                                 const double* axb, HxDev hx, int* err,
+                                                 int64_t j0, int64_t j1) {
+  const int64_t j = j0 + (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x / 32);
+  if (j >= j1) return;
   const unsigned lane = threadIdx.x & 31u;
   const int k = g.ens, n = g.n;
   const int o = ob.copy_obs[j];
@@ -240,11 +243,70 @@ __global__ void __launch_bounds__(128) hx_kernel(Geometry g, ObsDev ob, const do
 }
 
 void launch_hx(const Geometry& g, const ObsDev& o, const double* xb, const double* axb,
-               HxDev hx, int* err, cudaStream_t stream) {
-  if (o.n_copies == 0) return;
+               HxDev hx, int* err, cudaStream_t stream, int64_t j0, int64_t j1) {
+  if (j1 < 0 || j1 > o.n_copies) j1 = o.n_copies;
+  if (j0 < 0) j0 = 0;
+  if (j1 <= j0) return;
   const int warps = 4;
-  const int64_t blocks = (o.n_copies + warps - 1) / warps;
-  hx_kernel<<<(unsigned)blocks, 32 * warps, 0, stream>>>(g, o, xb, axb, hx, err);
+  const int64_t blocks = (j1 - j0 + warps - 1) / warps;
+  hx_kernel<<<(unsigned)blocks, 32 * warps, 0, stream>>>(g, o, xb, axb, hx, err, j0, j1);
+}
+
+// Packed H(x) rows, ens + 3 doubles per entry (yb[0 .. ens), dis, ln p,
+// rdiaginv): the unit of the observation exchange between column shards (the
+// role of comm_obs_data, x86/DA/LETKF/src/letkf_obs.F90:251-466).  One thread
+// per row element; consecutive threads take consecutive elements.
+__global__ void hx_export_kernel(int k, int64_t e0, int64_t nrows, HxDev hx, double* rows) {
+  const int64_t w = k + 3, total = nrows * w;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / w;
+    const int c = (int)(i - r * w);
+    const int64_t e = e0 + r;
+    double v;
+    if (c < k) v = hx.yb[(size_t)e * k + c];
+    else if (c == k) v = hx.dis[e];
+    else if (c == k + 1) v = hx.lnp[e];
+    else v = (double)hx.rdiag[e];  // exact
+    rows[i] = v;
+  }
+}
+
+__global__ void hx_import_kernel(int k, int64_t e0, int64_t nrows, HxDev hx, const double* rows) {
+  const int64_t w = k + 3, total = nrows * w;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / w;
+    const int c = (int)(i - r * w);
+    const int64_t e = e0 + r;
+    const double v = rows[i];
+    if (c < k) {
+      hx.yb[(size_t)e * k + c] = v;
+      if (hx.yb32) hx.yb32[(size_t)e * k + c] = (float)v;  // as hx_kernel rounds it
+    } else if (c == k) {
+      hx.dis[e] = v;
+    } else if (c == k + 1) {
+      hx.lnp[e] = v;
+    } else {
+      hx.rdiag[e] = (float)v;  // a float value: exact
+    }
+  }
+}
+
+void launch_hx_export(int ens, int64_t e0, int64_t e1, const HxDev& hx, double* rows,
+                      cudaStream_t stream) {
+  if (e1 <= e0) return;
+  const int64_t total = (e1 - e0) * (ens + 3);
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
+  hx_export_kernel<<<blocks, 256, 0, stream>>>(ens, e0, e1 - e0, hx, rows);
+}
+
+void launch_hx_import(int ens, int64_t e0, int64_t e1, HxDev hx, const double* rows,
+                      cudaStream_t stream) {
+  if (e1 <= e0) return;
+  const int64_t total = (e1 - e0) * (ens + 3);
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
+  hx_import_kernel<<<blocks, 256, 0, stream>>>(ens, e0, e1 - e0, hx, rows);
 }
 
 __global__ void nan_check_kernel(const double* x, size_t n, int* err) {

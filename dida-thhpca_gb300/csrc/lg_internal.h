@@ -160,8 +160,16 @@ void launch_cell_cands(const ObsDev& o, double obs_polar, const int* slot_obs, i
 void launch_obs_trig(const ObsDev& o, double* dcx, double* dsx, double* dyr, float* fcx,
                      float* fsx, float* fyr, cudaStream_t stream);
 void set_type_table(const TypeTable& t, cudaStream_t stream);
+// H(x) of the block copies [j0, j1) (j1 < 0: through the last copy)
 void launch_hx(const Geometry& g, const ObsDev& o, const double* xb, const double* axb,
-               HxDev hx, int* err, cudaStream_t stream);
+               HxDev hx, int* err, cudaStream_t stream, int64_t j0 = 0, int64_t j1 = -1);
+// H(x) rows of entries [e0, e1) packed as ens + 3 doubles each -- yb[ens], dis,
+// ln p, rdiaginv -- out of (export) or into (import; also the FP32 operand copy
+// of yb on the mixed path) the context's H(x) buffers
+void launch_hx_export(int ens, int64_t e0, int64_t e1, const HxDev& hx, double* rows,
+                      cudaStream_t stream);
+void launch_hx_import(int ens, int64_t e0, int64_t e1, HxDev hx, const double* rows,
+                      cudaStream_t stream);
 void launch_search(const Geometry& g, const ObsDev& o, ListDev l, int fill,
                    unsigned long long* band, cudaStream_t stream);
 void launch_search_cells(const Geometry& g, const ObsDev& o, const CellIndex& ci, ListDev l,
@@ -200,8 +208,9 @@ void launch_gram_col(const Geometry& g, const HxDev& hx, const ListDev& l, const
 void launch_gram_tc_stream(const Geometry& g, const HxDev& hx, const ListDev& l,
                            const SolveBatch& b, const double* axb, double* C, double* t, int* err,
                            const RecDev& rec, cudaStream_t stream);
-void launch_records(int ncol, const ListDev& l, const HxDev& hx, float lo, float inv_dz, int nb,
-                    int* boff, float4* rec, cudaStream_t stream);
+// records of the columns col0 .. col0 + ncol - 1
+void launch_records(int col0, int ncol, const ListDev& l, const HxDev& hx, float lo, float inv_dz,
+                    int nb, int* boff, float4* rec, cudaStream_t stream);
 // Cube solves (da_block_interval cube_n, da_vertical_interval cube_nz,
 // da_block_overlap): cubes of cube_n x cube_n columns of a block, stepping by
 // stride = cube_n - overlap from each block's first column, numbered block by

@@ -14,6 +14,7 @@
 // latlon_dist_r8 (pro_info.F90:149-161) evaluated without contraction, so the
 // kept set and its order equal the reference's.  Two passes: count, then fill
 // at the prefix-summed offsets.
+#include <cuda/std/functional>
 #include <cub/device/device_scan.cuh>
 
 #include "lg_device.cuh"
@@ -136,9 +137,14 @@ void launch_search(const Geometry& g, const ObsDev& o, ListDev l, int fill,
   search_kernel<<<(nc + warps - 1) / warps, 32 * warps, 0, stream>>>(g, o, l, fill, sa, band);
 }
 
+// The scan accumulates in 64 bits: ExclusiveSum would add the int counts in
+// int (its accumulator is the input's value type), and a list of more than
+// 2^31 entries (a large globe, or a window of one) would wrap.  An int64_t
+// initial value makes the accumulator int64_t.
 size_t scan_tmp_bytes(int n) {
   size_t bytes = 0;
-  cub::DeviceScan::ExclusiveSum(nullptr, bytes, (const int*)nullptr, (int64_t*)nullptr, n + 1);
+  cub::DeviceScan::ExclusiveScan(nullptr, bytes, (const int*)nullptr, (int64_t*)nullptr,
+                                 ::cuda::std::plus<int64_t>{}, (int64_t)0, n + 1);
   return bytes;
 }
 
@@ -146,7 +152,8 @@ size_t scan_tmp_bytes(int n) {
 // extra element, so the caller keeps cnt sized n+1 with cnt[n] = 0)
 void launch_scan_counts(const int* cnt, int64_t* off, int n, void* tmp, size_t tmp_bytes,
                         cudaStream_t stream) {
-  cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, cnt, off, n + 1, stream);
+  cub::DeviceScan::ExclusiveScan(tmp, tmp_bytes, cnt, off, ::cuda::std::plus<int64_t>{},
+                                 (int64_t)0, n + 1, stream);
 }
 
 }  // namespace lg
@@ -162,14 +169,16 @@ namespace lg {
 // contiguous bucket range, so each solve scans only its window instead of the
 // whole list.  One warp per column; the ranking inside a bucket uses the lane
 // order, so the layout is deterministic.
-__global__ void __launch_bounds__(128) records_kernel(int ncol, ListDev l, HxDev hx, float lo,
-                                                      float inv_dz, int nb, int* boff, float4* rec) {
+__global__ void __launch_bounds__(128) records_kernel(int col0, int ncol, ListDev l, HxDev hx,
+                                                      float lo, float inv_dz, int nb, int* boff,
+                                                      float4* rec) {
   const int warps = blockDim.x / 32;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int col = blockIdx.x * warps + w;
+  const int idx = blockIdx.x * warps + w;
   extern __shared__ int cur_all[];
   int* cur = cur_all + w * (nb + 1);
-  if (col >= ncol) return;
+  if (idx >= ncol) return;
+  const int col = col0 + idx;
   for (int b = lane; b <= nb; b += 32) cur[b] = 0;
   __syncwarp();
   const int64_t base = l.off[col];
@@ -219,12 +228,13 @@ __global__ void __launch_bounds__(128) records_kernel(int ncol, ListDev l, HxDev
   }
 }
 
-void launch_records(int ncol, const ListDev& l, const HxDev& hx, float lo, float inv_dz, int nb,
-                    int* boff, float4* rec, cudaStream_t stream) {
+void launch_records(int col0, int ncol, const ListDev& l, const HxDev& hx, float lo,
+                    float inv_dz, int nb, int* boff, float4* rec, cudaStream_t stream) {
+  if (ncol <= 0) return;
   const int warps = 4;
   const size_t smem = sizeof(int) * warps * (nb + 1);
   records_kernel<<<(ncol + warps - 1) / warps, 32 * warps, smem, stream>>>(
-      ncol, l, hx, lo, inv_dz, nb, boff, rec);
+      col0, ncol, l, hx, lo, inv_dz, nb, boff, rec);
 }
 
 }  // namespace lg

@@ -363,6 +363,14 @@ def load_library(path: str = LIB_PATH):
                                        P(C.c_double), P(C.c_double), P(C.c_double),
                                        P(C.c_double)]
     lib.lg_core_batch_noalloc.argtypes = lib.lg_core_batch.argtypes
+    lib.lg_set_columns.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    lib.lg_list_counts.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int64)]
+    lib.lg_set_shard.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    lib.lg_shard_entries.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64), P(C.c_int64)]
+    lib.lg_hx_device.argtypes = [C.c_void_p] * 4
+    lib.lg_hx_export.argtypes = [C.c_void_p] * 3
+    lib.lg_hx_import.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p]
+    lib.lg_analyse_device.argtypes = [C.c_void_p] * 6
     lib.lg_status_string.restype = C.c_char_p
     lib.lg_status_string.argtypes = [C.c_int]
     _lib = lib
@@ -452,6 +460,64 @@ class Letkf:
         check(self.lib.lg_run_device(self.h, ntimes, C.c_void_p(xb.data_ptr()),
                                      C.c_void_p(axb.data_ptr()), C.c_void_p(xa.data_ptr()),
                                      C.c_void_p(axa.data_ptr()), s), "lg_run_device")
+
+    # ------------------------------------------------ windows and shards
+    def set_columns(self, col_begin: int, col_end: int):
+        """Analyse only columns [col_begin, col_end) (c = lon * num_lat + lat, 0-based)."""
+        check(self.lib.lg_set_columns(self.h, col_begin, col_end), "lg_set_columns")
+
+    def list_counts(self) -> np.ndarray:
+        """Local entries of every column's list (the count pass only)."""
+        counts = np.zeros(self.cfg.num_lat * self.cfg.num_lon, np.int32)
+        total = C.c_int64()
+        check(self.lib.lg_list_counts(self.h, _ptr(counts, C.c_int), C.byref(total)),
+              "lg_list_counts")
+        return counts
+
+    def windows(self, max_entries: int):
+        """Column windows [(c0, c1), ...] covering the globe in order, each of
+        whole longitudes and at most max_entries list entries (a longitude
+        above the budget is a window of its own)."""
+        cnt = self.list_counts().reshape(self.cfg.num_lon, self.cfg.num_lat).sum(axis=1)
+        out, start, acc = [], 0, 0
+        for lon, c in enumerate(cnt):
+            if acc and acc + c > max_entries:
+                out.append((start * self.cfg.num_lat, lon * self.cfg.num_lat))
+                start, acc = lon, 0
+            acc += int(c)
+        out.append((start * self.cfg.num_lat, self.cfg.num_lon * self.cfg.num_lat))
+        return out
+
+    def set_shard(self, lon_block_begin: int, lon_block_end: int):
+        """This context's shard: longitude blocks [begin, end) of the virtual decomposition."""
+        check(self.lib.lg_set_shard(self.h, lon_block_begin, lon_block_end), "lg_set_shard")
+
+    def shard_entries(self):
+        """(entry_begin, entry_end, n_entries): the shard's own H(x) entries."""
+        a, b, n = C.c_int64(), C.c_int64(), C.c_int64()
+        check(self.lib.lg_shard_entries(self.h, C.byref(a), C.byref(b), C.byref(n)),
+              "lg_shard_entries")
+        return a.value, b.value, n.value
+
+    def hx_device(self, xb, axb, stream=None):
+        s = C.c_void_p(stream) if stream is not None else None
+        check(self.lib.lg_hx_device(self.h, C.c_void_p(xb.data_ptr()), C.c_void_p(axb.data_ptr()),
+                                    s), "lg_hx_device")
+
+    def hx_export(self, rows, stream=None):
+        """rows: CUDA float64 tensor of (entry_end - entry_begin) x (ens + 3)."""
+        s = C.c_void_p(stream) if stream is not None else None
+        check(self.lib.lg_hx_export(self.h, C.c_void_p(rows.data_ptr()), s), "lg_hx_export")
+
+    def hx_import(self, rows, entry_begin: int, entry_end: int, stream=None):
+        s = C.c_void_p(stream) if stream is not None else None
+        check(self.lib.lg_hx_import(self.h, C.c_void_p(rows.data_ptr()), entry_begin, entry_end,
+                                    s), "lg_hx_import")
+
+    def analyse_device(self, xb, axb, xa, axa, stream=None):
+        s = C.c_void_p(stream) if stream is not None else None
+        check(self.lib.lg_analyse_device(self.h, *[C.c_void_p(t.data_ptr()) for t in
+                                                   (xb, axb, xa, axa)], s), "lg_analyse_device")
 
     def run_da_parallel(self, ntimes: int, gamma1: float, gamma2: float, polar_lat: float,
                         xb_in: np.ndarray, xa_out: np.ndarray, spread_b: np.ndarray,

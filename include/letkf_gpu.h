@@ -175,6 +175,57 @@ int lg_run(lg_ctx* ctx, int ntimes, const double* xb, const double* axb, double*
 int lg_run_device(lg_ctx* ctx, int ntimes, const double* d_xb, const double* d_axb,
                   double* d_xa, double* d_axa, void* stream);
 
+/* Column windows and column shards.  The reference spreads the globe over a
+ * 2-D grid of MPI ranks, each analysing its own block of columns after one
+ * exchange of observations with its neighbour blocks (comm_obs_data,
+ * x86/DA/LETKF/src/letkf_obs.F90:251-466; decomposition
+ * x86/DA/EnDNN/src/module_da_parallel.F90:75-109).  Here one context holds
+ * the whole globe's geometry and observations, and an analysis can be
+ * restricted to a range of columns:
+ *
+ * lg_set_columns: analyse only grid columns [col_begin, col_end) (column
+ *   c = (lon-1)*num_lat + (lat-1)); neighbour lists, solves and xa/axa values
+ *   are produced for those columns alone (lg_run copies out only them) and
+ *   the lists' device memory scales with the range, so a large globe can be
+ *   analysed window by window.  H(x) of lg_run* still covers every
+ *   observation copy.  LG_ERR_UNSUPPORTED with cubes.
+ * lg_set_shard: the shard of a column-sharded analysis: longitude blocks
+ *   [lon_block_begin, lon_block_end) of the virtual decomposition (0-based),
+ *   i.e. their columns at every latitude, plus the block copies of those
+ *   blocks as the shard's own observations (lg_shard_entries gives their
+ *   entry range).  One shard per process and GPU; the shards of a run
+ *   partition the longitude blocks.
+ * A sharded analysis step, per process:
+ *   lg_hx_device(own background)   H(x) of the shard's own copies; the
+ *                                  background must be valid on the shard's
+ *                                  columns and their halo
+ *   lg_hx_export(rows)             the own entries' H(x) rows, ens + 3 doubles
+ *                                  each (yb[ens], innovation, ln p, rdiaginv)
+ *   (caller: all-gather of the rows of every shard, e.g. over NCCL)
+ *   lg_hx_import(rows of shard r, its entry range)  for every other shard
+ *   lg_analyse_device(...)         selection and solves of the shard's columns
+ *                                  with the H(x) now in the context
+ * lg_run_device with a shard set recomputes H(x) of every copy from the
+ * background it is given and analyses the shard's columns.  All of these
+ * enqueue on the stream (NULL: the context's own) and, except the export and
+ * import, synchronise with it before returning. */
+int lg_set_columns(lg_ctx* ctx, int col_begin, int col_end);
+/* Local entries of every column's neighbour list for the current observation
+ * set (the selection's count pass alone; nothing is stored): counts has
+ * num_lat*num_lon ints, *total (optional) their sum.  For planning windows
+ * whose lists fit a memory budget (each entry costs 12 bytes, 28 in mixed
+ * precision).  LG_ERR_UNSUPPORTED with cubes. */
+int lg_list_counts(lg_ctx* ctx, int* counts, int64_t* total);
+int lg_set_shard(lg_ctx* ctx, int lon_block_begin, int lon_block_end);
+int lg_shard_entries(const lg_ctx* ctx, int64_t* entry_begin, int64_t* entry_end,
+                     int64_t* n_entries);
+int lg_hx_device(lg_ctx* ctx, const double* d_xb, const double* d_axb, void* stream);
+int lg_hx_export(const lg_ctx* ctx, double* d_rows, void* stream);
+int lg_hx_import(lg_ctx* ctx, const double* d_rows, int64_t entry_begin, int64_t entry_end,
+                 void* stream);
+int lg_analyse_device(lg_ctx* ctx, const double* d_xb, const double* d_axb, double* d_xa,
+                      double* d_axa, void* stream);
+
 /* The DA caller's pre-processing around letkf_run (run_da_parallel,
  * x86/DA/EnDNN/src/module_da_parallel.F90:186-211), device arrays over the whole
  * globe with halo: axb = sum(xb_in)/real(ens), xb = xb_in - axb.  Returns

@@ -683,6 +683,63 @@ int or_hx(or_ctx* c, const double* xb, const double* axb, int nthreads) {
   return status;
 }
 
+/* H(x) of the block copies [j0, j1) only (one shard's own copies); the other
+ * entries keep what they hold (set them with or_set_hx_rows) */
+int or_hx_range(or_ctx* c, const double* xb, const double* axb, int64_t j0, int64_t j1,
+                int nthreads) {
+  const int ens = c->cfg.ens, nz = c->cfg.nz;
+  if (j0 < 0 || j1 > c->n_copies || j0 > j1) return LG_ERR_ARG;
+  int maxonz = 1;
+  for (int t = 0; t < c->n_types; ++t)
+    if (c->types[t].nz > maxonz) maxonz = c->types[t].nz;
+  int status = LG_OK;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+#endif
+  {
+    double* xb_ph = (double*)malloc(sizeof(double) * ens * (nz + 1));
+    int* ph_pos = (int*)malloc(sizeof(int) * ens * maxonz);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 256)
+#endif
+    for (int64_t j = j0; j < j1; ++j) {
+      int s = hx_copy(c, j, xb, axb, xb_ph, ph_pos);
+      if (s != LG_OK) status = s;
+    }
+    free(xb_ph);
+    free(ph_pos);
+  }
+  c->hx_done = (status == LG_OK);
+  return status;
+}
+
+/* H(x) rows of entries [e0, e1), ens + 2 doubles each: yb[ens], dis, ln p */
+int or_get_hx_rows(const or_ctx* c, double* rows, int64_t e0, int64_t e1) {
+  const int ens = c->cfg.ens;
+  if (e0 < 0 || e1 > c->n_entries || e0 > e1) return LG_ERR_ARG;
+  for (int64_t e = e0; e < e1; ++e) {
+    double* r = rows + (size_t)(e - e0) * (ens + 2);
+    memcpy(r, c->yb + (size_t)e * ens, sizeof(double) * ens);
+    r[ens] = c->dis[e];
+    r[ens + 1] = c->lnp[e];
+  }
+  return LG_OK;
+}
+
+int or_set_hx_rows(or_ctx* c, const double* rows, int64_t e0, int64_t e1) {
+  const int ens = c->cfg.ens;
+  if (e0 < 0 || e1 > c->n_entries || e0 > e1) return LG_ERR_ARG;
+  for (int64_t e = e0; e < e1; ++e) {
+    const double* r = rows + (size_t)(e - e0) * (ens + 2);
+    memcpy(c->yb + (size_t)e * ens, r, sizeof(double) * ens);
+    c->dis[e] = r[ens];
+    c->lnp[e] = r[ens + 1];
+  }
+  c->hx_done = 1;
+  return LG_OK;
+}
+
 int or_get_hx(const or_ctx* c, double* yb, double* dis, double* lnp) {
   if (!c->hx_done) return LG_ERR_STATE;
   if (yb) memcpy(yb, c->yb, sizeof(double) * c->n_entries * c->cfg.ens);

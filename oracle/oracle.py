@@ -47,6 +47,10 @@ def lib(use_lapack: bool = True):
     L.or_destroy.restype = None
     L.or_hx.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), C.c_int]
     L.or_get_hx.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), P(C.c_double)]
+    L.or_hx_range.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), C.c_int64, C.c_int64,
+                              C.c_int]
+    L.or_get_hx_rows.argtypes = [C.c_void_p, P(C.c_double), C.c_int64, C.c_int64]
+    L.or_set_hx_rows.argtypes = [C.c_void_p, P(C.c_double), C.c_int64, C.c_int64]
     L.or_n_copies.restype = C.c_int64
     L.or_n_copies.argtypes = [C.c_void_p]
     L.or_n_entries.restype = C.c_int64
@@ -125,6 +129,24 @@ class Oracle:
         lnp = np.zeros(self.n_entries)
         lib().or_get_hx(self.h, _p(yb, C.c_double), _p(dis, C.c_double), _p(lnp, C.c_double))
         return yb, dis, lnp
+
+    def hx_range(self, xb, axb, j0: int, j1: int, nthreads: int = 0):
+        """H(x) of the block copies [j0, j1) only."""
+        st = lib().or_hx_range(self.h, _p(xb, C.c_double), _p(axb, C.c_double), j0, j1, nthreads)
+        if st != 0:
+            raise RuntimeError(f"or_hx_range: {st}")
+
+    def hx_rows(self, e0: int, e1: int):
+        """H(x) rows of entries [e0, e1): (e1 - e0) x (ens + 2) -- yb, dis, ln p."""
+        rows = np.zeros((max(0, e1 - e0), self.cfg.ens + 2))
+        if lib().or_get_hx_rows(self.h, _p(rows, C.c_double), e0, e1) != 0:
+            raise RuntimeError("or_get_hx_rows")
+        return rows
+
+    def set_hx_rows(self, rows, e0: int, e1: int):
+        rows = np.ascontiguousarray(rows, np.float64)
+        if lib().or_set_hx_rows(self.h, _p(rows, C.c_double), e0, e1) != 0:
+            raise RuntimeError("or_set_hx_rows")
 
     def copy_layout(self):
         co = np.zeros(max(1, self.n_copies), np.int32)

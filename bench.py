@@ -12,6 +12,10 @@ e2e   : the same metric through the host-array call a DA driver makes
         (lg_set_obs + lg_run with pinned host buffers: observation ingest and the
         background H2D copy, analysis D2H copy inside the timed region).
 e2e is the median over its steps.
+contraction_variants : (mixed runs, N <= 64) the same workload with the Gram
+        contractions as TF32 hi/lo tensor-core products (LG_PREC_MIXED_TF32, the
+        FP32 variant) beside the timed BF16 hi/lo ones, each with its time and
+        its increment error against plain FP64.
 fp64  : (mixed runs) after the timed mixed analyses, the plain-FP64 GPU path on
         the same inputs: its time per analysis, the speed-up of the mixed path
         over it, and the mixed analysis' per-variable increment error against it
@@ -62,7 +66,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg3")
-    ap.add_argument("--precision", default=None, choices=[None, "fp64", "mixed"])
+    ap.add_argument("--precision", default=None, choices=[None, "fp64", "mixed", "tf32"])
+    ap.add_argument("--no-tf32", action="store_true",
+                    help="skip the TF32 (FP32-variant) Gram beside the BF16 one")
+    ap.add_argument("--variant-steps", type=int, default=3,
+                    help="timed analyses of the TF32 variant (after one untimed one)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the bounded oracle sample")
@@ -367,7 +375,8 @@ def main():
 
     cfg = lg.preset(args.config)
     if args.precision:
-        cfg = cfg.replace(precision=lg.LG_PREC_MIXED if args.precision == "mixed" else lg.LG_PREC_FP64)
+        cfg = cfg.replace(precision={"mixed": lg.LG_PREC_MIXED, "tf32": lg.LG_PREC_MIXED_TF32,
+                                     "fp64": lg.LG_PREC_FP64}[args.precision])
     w = synth.make_workload(cfg, backend="torch", device=dev)
     ncol = cfg.num_lat * cfg.num_lon
     ctx = lg.Letkf(cfg)
@@ -388,7 +397,7 @@ def main():
         shard_cols = shard.shard_columns(cfg, by_range)
     # column windows when the whole globe's neighbour lists (12 bytes an entry,
     # 28 with the mixed path's Gram records) exceed the list budget
-    mixed = cfg.precision == lg.LG_PREC_MIXED
+    mixed = cfg.precision in (lg.LG_PREC_MIXED, lg.LG_PREC_MIXED_TF32)
     bytes_per_entry = 28 if mixed else 12
     windows = [(0, ncol)]
     if not dist:
@@ -463,6 +472,30 @@ def main():
     fp64_arm = mixed and not args.no_fp64 and world == 1
     if fp64_arm:
         xa_mixed, axa_mixed = xa.clone(), axa.clone()
+    # the other tensor-core contraction on the same workload (BF16 hi/lo and
+    # TF32 hi/lo, the FP32 variant, side by side), timed outside the main region
+    variants = {}
+    if (cfg.precision == lg.LG_PREC_MIXED and not args.no_tf32 and world == 1
+            and len(windows) == 1 and cfg.ens <= 64):
+        ctx_v = lg.Letkf(cfg.replace(precision=lg.LG_PREC_MIXED_TF32))
+        ctx_v.set_obs(w.obs)
+        xa_v, axa_v = torch.zeros_like(xa), torch.zeros_like(axa)
+        ctx_v.letkf_run_device(0, xb, axb, xa_v, axa_v, stream.cuda_stream)
+        torch.cuda.synchronize()
+        v0 = torch.cuda.Event(enable_timing=True)
+        v1 = torch.cuda.Event(enable_timing=True)
+        v0.record(stream)
+        for _ in range(args.variant_steps):
+            ctx_v.letkf_run_device(0, xb, axb, xa_v, axa_v, stream.cuda_stream)
+        v1.record(stream)
+        torch.cuda.synchronize()
+        ms_v = v0.elapsed_time(v1) / args.variant_steps
+        st_v = ctx_v.stats()
+        ctx_v.letkf_final()
+        variants["tf32"] = {"ms_per_step": ms_v, "value": ncol / (ms_v * 1e-3),
+                            "ms_gram_last": st_v["ms_gram"], "xa": (xa_v, axa_v)}
+        variants["bf16"] = {"ms_per_step": ms, "value": value,
+                            "xa": (xa_mixed, axa_mixed) if fp64_arm else None}
 
     # Per-kernel durations without overlap: one more analysis on a single solve
     # stream (outside the timed region) gives every kernel its own event time;
@@ -531,14 +564,17 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "strong" if world > 1 else "weak",
         "vs_baseline": None,
-        "dtype": "bf16/f32 contractions, f64 eig" if cfg.precision == lg.LG_PREC_MIXED else "f64",
+        "dtype": {lg.LG_PREC_MIXED: "bf16/f32 contractions, f64 eig",
+                  lg.LG_PREC_MIXED_TF32: "tf32/f32 contractions, f64 eig",
+                  lg.LG_PREC_FP64: "f64"}[cfg.precision],
         "data": "synthetic (seeded spherical-harmonic ensemble, %s observations)" % (
             "uniform" if not cfg.clustered_frac else
             f"{int(100 * cfg.clustered_frac)}% clustered + uniform"),
         "config": {"workload": f"{cfg.name}: {cfg.num_lon}x{cfg.num_lat}x{cfg.nz}, ps/u/v/pt, "
                                f"N={cfg.ens}, {cfg.n_obs} obs, L={cfg.local_dist:g} km, "
                                f"vert {cfg.vert_dist:g} ln p, rho={cfg.inflation}",
-                   "precision": "mixed" if cfg.precision == lg.LG_PREC_MIXED else "fp64",
+                   "precision": {lg.LG_PREC_MIXED: "mixed", lg.LG_PREC_MIXED_TF32: "mixed-tf32",
+                                 lg.LG_PREC_FP64: "fp64"}[cfg.precision],
                    "columns": ncol, "solves_per_step": st["n_solves"],
                    "list_entries_per_step": st["nobsl_total"],
                    "gram_entries_per_step": iso["n_gram_entries"],
@@ -664,6 +700,12 @@ def main():
         ms_mixed = ms if len(windows) == 1 else win_ms[len(windows) // 2]
         errs = increment_rel_rms(cfg, xb, axb, (xa_mixed, axa_mixed), (xa, axa),
                                  None if len(windows) == 1 else lons)
+        for vd in variants.values():
+            if vd.get("xa") is not None:
+                ev = increment_rel_rms(cfg, xb, axb, vd["xa"], (xa, axa))
+                vd["increment_rel_rms"] = ev
+                vd["increment_rel_rms_max"] = max(ev.values())
+                vd["speedup_vs_fp64"] = ms64 / vd["ms_per_step"]
         line["fp64"] = {
             "ms_per_step": ms64, "steps": args.fp64_steps, "value": (wb - wa) / (ms64 * 1e-3),
             "columns": wb - wa, "mixed_ms_same_columns": ms_mixed,
@@ -691,6 +733,12 @@ def main():
         v, info = cpu_sample(cfg, w.obs, xb_h, axb_h, args.cpu_seconds, nthreads)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
                                 "sample": info["sample"] + "; " + info["lapack"]}
+    if variants:
+        line["contraction_variants"] = {
+            name: {kk: v for kk, v in vd.items() if kk != "xa"} for name, vd in variants.items()}
+        line["contraction_variants_note"] = (
+            "the Gram contractions as BF16 hi/lo (the timed value) and as TF32 hi/lo tensor-core "
+            "products (the FP32 variant), same workload; errors against the plain-FP64 analysis")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ctx is not None:

@@ -416,7 +416,7 @@ int ensure_hx(lg_ctx* c, size_t entries) {
   const size_t k = (size_t)c->cfg.ens;
   int r = LG_OK;
   r |= dalloc(&c->hx.yb, cap * k);
-  if (c->cfg.precision == LG_PREC_MIXED) r |= dalloc(&c->hx.yb32, cap * k);
+  if (lg::mixed_precision(c->cfg.precision)) r |= dalloc(&c->hx.yb32, cap * k);
   r |= dalloc(&c->hx.dis, cap);
   r |= dalloc(&c->hx.lnp, cap);
   r |= dalloc(&c->hx.rdiag, cap);
@@ -481,7 +481,10 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
     return LG_ERR_ARG;
   // cubes (letkf_compute.F90): the loops step by cube_n - overlap
   if (g.cube_n < 1 || g.cube_nz < 1 || g.overlap < 0 || g.overlap >= g.cube_n) return LG_ERR_ARG;
-  if (g.precision != LG_PREC_FP64 && g.precision != LG_PREC_MIXED) return LG_ERR_ARG;
+  if (g.precision != LG_PREC_FP64 && !lg::mixed_precision(g.precision)) return LG_ERR_ARG;
+  // the TF32 Gram holds [hi; lo] of every member in one M = 128 operand
+  if (g.precision == LG_PREC_MIXED_TF32 && !lg::gram_tf32_supported(g.ens))
+    return LG_ERR_UNSUPPORTED;
   int rows = 0;
   for (int v = 0; v < g.n_var; ++v) {
     if (g.var_lev[v] != 1 && g.var_lev[v] != g.nz) return LG_ERR_SHAPE;
@@ -963,7 +966,7 @@ float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
 // mixed precision cube solves form their trans in FP32 from the tridiagonal
 // form and the QL rotation log (trans_kernel); FP64 ones with eig_apply
 bool cube_trans_fp32(const lg_ctx* c) {
-  return c->cfg.precision == LG_PREC_MIXED && c->cfg.ens <= 64;
+  return lg::mixed_precision(c->cfg.precision) && c->cfg.ens <= 64;
 }
 
 int build_cube_plan(lg_ctx* c) {
@@ -1074,7 +1077,7 @@ int prepare_capacity(lg_ctx* c) {
     c->list_cap = cap;
   }
   c->list_total = total;
-  const bool mixed_tc = g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k);
+  const bool mixed_tc = lg::mixed_precision(g.precision) && lg::gram_tc_supported(k);
   if (mixed_tc && (c->rec_cap < c->list_cap || !c->d_boff || c->boff_nb != c->tune.lnp_buckets)) {
     dfree(c->d_rec); dfree(c->d_boff);
     int r = LG_OK;
@@ -1148,7 +1151,7 @@ int prepare_capacity(lg_ctx* c) {
   const int nl = c->tune.solve_streams;
   // rotation log entries: (cos, sin) as two doubles, or two floats where only
   // the FP32 vector kernel replays them (mixed precision)
-  const size_t rot_pairs_per_slot = g.precision == LG_PREC_MIXED ? 2 : 1;
+  const size_t rot_pairs_per_slot = lg::mixed_precision(g.precision) ? 2 : 1;
   for (int li = 0; li < 4; ++li) {
     lg_ctx::SolveLane& L = c->lane[li];
     const size_t cap = li < nl ? (size_t)c->chunk * levels : 0;
@@ -1296,7 +1299,7 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   launches += 1;
   CK(record_event(c->ev[5], st));
   CK(cudaStreamWaitEvent(st, c->ev_hx, 0));
-  const bool mixed_tc = g.precision == LG_PREC_MIXED && lg::gram_tc_supported(k);
+  const bool mixed_tc = lg::mixed_precision(g.precision) && lg::gram_tc_supported(k);
   lg::RecDev rec{};
   if (mixed_tc) {
     const int nb = c->tune.lnp_buckets;
@@ -1347,7 +1350,9 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
       b.nsolves = std::min(cs, ns - q * cs);
       b.work = c->d_work;
       CK(record_event(kv[0], st));
-      if (mixed_tc)
+      if (g.precision == LG_PREC_MIXED_TF32)
+        lg::launch_gram_tf32(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec, st);
+      else if (mixed_tc)
         lg::launch_gram_tc_stream(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec, st);
       else
         lg::launch_gram64(geo, c->hx, c->lists, b, axb, L.C, L.t, st);
@@ -1436,7 +1441,7 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     if (nl >= 3) CK(cudaStreamWaitEvent(c->third_stream, c->ev_fork, 0));
     if (nl == 4) CK(cudaStreamWaitEvent(c->fourth_stream, c->ev_fork, 0));
   }
-  const bool fp32_vec = g.precision == LG_PREC_MIXED;
+  const bool fp32_vec = lg::mixed_precision(g.precision);
   for (int q = 0; q < nchunks; ++q) {
     const int set = q % nl;
     lg_ctx::SolveLane& L = c->lane[set];
@@ -1455,7 +1460,9 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     // Gram (phase pipeline: after the buffer set's previous vector update)
     if (nl >= 3 && q >= nl) CK(cudaStreamWaitEvent(s_g, c->ev_phase[3][set], 0));
     CK(record_event(kv[0], s_g));
-    if (mixed_tc && (gram_kind == GramKind::kColumn || gram_kind == GramKind::kColumnLean))
+    if (g.precision == LG_PREC_MIXED_TF32)
+      lg::launch_gram_tf32(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec, s_g);
+    else if (mixed_tc && (gram_kind == GramKind::kColumn || gram_kind == GramKind::kColumnLean))
       lg::launch_gram_col(geo, c->hx, c->lists, b, axb, L.C, L.t, c->d_status, rec,
                           gram_kind == GramKind::kColumnLean, c->tune.gram_ctas, s_g);
     else if (mixed_tc && gram_kind == GramKind::kStream)
@@ -1923,7 +1930,7 @@ int lg_autotune(lg_ctx* c, const double* xb, const double* axb, double* xa, doub
   if (!c || !xb || !axb || !xa || !axa || !best) return LG_ERR_ARG;
   if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
   const lg_config& g = c->cfg;
-  const bool mixed = g.precision == LG_PREC_MIXED;
+  const bool mixed = g.precision == LG_PREC_MIXED;  // the BF16 Gram variants to tune
   const bool vertical = g.vert_dist > 0.0;
   lg_tuning cur = c->tune;
   if (cur.gram_kernel == LG_GRAM_AUTO)
@@ -2153,7 +2160,8 @@ int lg_core_batch(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
                   const double* d_rloc, double inflation, int precision, double* d_trans,
                   double* d_wbar, void* stream_v) {
   if (ens < 2 || ens > 128 || nbatch < 0 || inflation <= 0.0) return LG_ERR_ARG;
-  if (precision != LG_PREC_FP64 && precision != LG_PREC_MIXED) return LG_ERR_ARG;
+  if (precision != LG_PREC_FP64 && !lg::mixed_precision(precision)) return LG_ERR_ARG;
+  if (precision == LG_PREC_MIXED_TF32 && !lg::gram_tf32_supported(ens)) return LG_ERR_UNSUPPORTED;
   if (nbatch == 0) return LG_OK;
   if (!d_nobsl || !d_off || !d_trans || !d_wbar) return LG_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream_v;
@@ -2183,7 +2191,9 @@ int lg_core_batch(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
   cudaMemsetAsync(fail, 0, sizeof(int), st);
   lg::HxDev hx{};
   lg::ListDev l{};
-  if (precision == LG_PREC_MIXED && lg::gram_tc_supported(ens))
+  if (precision == LG_PREC_MIXED_TF32)
+    lg::launch_gram_tf32(geo, hx, l, b, nullptr, C, t, fail, lg::RecDev{}, st);
+  else if (precision == LG_PREC_MIXED && lg::gram_tc_supported(ens))
     lg::launch_gram_tc(geo, hx, l, b, nullptr, C, t, fail, st);
   else
     lg::launch_gram64(geo, hx, l, b, nullptr, C, t, st);
@@ -2193,6 +2203,8 @@ int lg_core_batch(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
       cudaMemcpyAsync(&h_fail, fail, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     result = LG_ERR_CUDA;
+  else if (h_fail < 0)
+    result = LG_ERR_TIMEOUT;  // a bounded tensor-core wait expired
   else if (h_fail)
     result = LG_ERR_EIG;
   dfree(C); dfree(t); dfree(fail);

@@ -153,6 +153,10 @@ __host__ __device__ inline void solve_col_level(const SolveBatch& b, int s, int&
   }
 }
 
+// the mixed-precision analysis path (tensor-core Gram, FP32 vector transform):
+// BF16 hi/lo (LG_PREC_MIXED) or TF32 hi/lo (LG_PREC_MIXED_TF32) contractions
+inline bool mixed_precision(int p) { return p == LG_PREC_MIXED || p == LG_PREC_MIXED_TF32; }
+
 // kernels (host launchers), all asynchronous on `stream`
 // cand[slot] of every copy slot (slot_obs[slot] = observation of the slot)
 void launch_cell_cands(const ObsDev& o, double obs_polar, const int* slot_obs, int nslots,
@@ -196,6 +200,12 @@ inline cudaError_t record_event(cudaEvent_t e, cudaStream_t st) {
              : cudaEventRecord(e, st);
 }
 bool gram_col_supported(int ens);
+// TF32 hi/lo per-solve tcgen05 Gram (LG_PREC_MIXED_TF32), ens <= 64; analysis
+// records (mode 0) or a core batch (mode 1)
+bool gram_tf32_supported(int ens);
+void launch_gram_tf32(const Geometry& g, const HxDev& hx, const ListDev& l, const SolveBatch& b,
+                      const double* axb, double* C, double* t, int* err, const RecDev& rec,
+                      cudaStream_t stream);
 // 65..128 members: per-solve tcgen05 Gram (analysis records or a core batch);
 // launch_gram_tc and launch_gram_tc_stream route these sizes to it
 bool gram_tc128_supported(int ens);

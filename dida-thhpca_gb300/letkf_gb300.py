@@ -29,6 +29,7 @@ LG_MAX_OBS_VARS = 8
 LG_OK = 0
 LG_PREC_FP64 = 0
 LG_PREC_MIXED = 1
+LG_PREC_MIXED_TF32 = 2
 LG_VCOORD_HYBRID = 0
 LG_VCOORD_SIGMA = 1
 

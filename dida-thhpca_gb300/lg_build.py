@@ -26,6 +26,7 @@ UNITS = {
     "lg_eig.cu": [],
     "lg_gram_tc.cu": [],
     "lg_gram_tc128.cu": [],
+    "lg_gram_tf32.cu": [],
     "lg_gram_col.cu": [],
     "lg_eig2.cu": [],
     "lg_noalloc.cu": [],

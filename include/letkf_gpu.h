@@ -62,6 +62,9 @@ extern "C" {
 /* precision of the analysis */
 #define LG_PREC_FP64 0   /* plain FP64 everywhere (parity path) */
 #define LG_PREC_MIXED 1  /* BF16 hi/lo tensor-core contractions, FP64 eigensolve */
+#define LG_PREC_MIXED_TF32 2 /* as LG_PREC_MIXED with the Gram contractions as TF32 hi/lo
+                                tensor-core products (about 2^-21 per operand instead of
+                                2^-16: the FP32 variant); ens <= 64 */
 
 /* vertical coordinate (da_vert_coord_init scheme) */
 #define LG_VCOORD_HYBRID 0  /* ph = a*(p0-ptop) + b*(ps-ptop) + ptop */
@@ -95,7 +98,7 @@ typedef struct lg_config {
                           cube_n - overlap and each column is the average over the cubes
                           covering it; as in the reference this path has no vertical
                           localisation (vert_dist is ignored) */
-  int precision;       /* LG_PREC_FP64 or LG_PREC_MIXED */
+  int precision;       /* LG_PREC_FP64, LG_PREC_MIXED or LG_PREC_MIXED_TF32 */
   int vcoord;          /* LG_VCOORD_HYBRID or LG_VCOORD_SIGMA */
 } lg_config;
 
@@ -378,7 +381,8 @@ void lg_destroy(lg_ctx* ctx);
  * for batch b with p_b = nobsl[b] entries starting at offset off[b]:
  *   hxens[(off[b]+j)*ens + i], rdiaginv[off[b]+j] (float), dep[off[b]+j], rloc[off[b]+j]
  *   -> trans[b*ens*ens + i + ens*j] (column-major ens x ens), wbar[b*ens + i].
- * precision: LG_PREC_FP64 or LG_PREC_MIXED.  stream: cudaStream_t or NULL. */
+ * precision: LG_PREC_FP64, LG_PREC_MIXED or LG_PREC_MIXED_TF32 (ens <= 64).
+ * stream: cudaStream_t or NULL. */
 int lg_core_batch(int ens, int nbatch, const int* d_nobsl, const int64_t* d_off,
                   const double* d_hxens, const float* d_rdiaginv, const double* d_dep,
                   const double* d_rloc, double inflation, int precision,

@@ -155,6 +155,82 @@ def test_mixed_128_members_on_tensor_cores_within_1e4(name):
     ctx.letkf_final()
 
 
+def test_core_batch_tf32_is_closer_to_fp64_than_bf16():
+    """The TF32 hi/lo Gram (LG_PREC_MIXED_TF32, the FP32 variant) keeps about
+    2^-21 of each operand against the BF16 split's 2^-16; with both
+    accumulating in FP32 (about sqrt(p) 2^-24), its trans and overline_w must
+    be clearly closer to the FP64 result, and within 2e-6 / 5e-6 of it."""
+    import ctypes as C
+    import torch
+    import letkf_gb300 as lg
+    from oracle import oracle as orc
+
+    rng = np.random.default_rng(23)
+    L = lg.load_library()
+    ptr = lambda x: C.c_void_p(x.data_ptr())  # noqa: E731
+    dev = torch.device("cuda")
+    for k, p in [(16, 5), (40, 300), (64, 2000), (64, 0)]:
+        hx = rng.standard_normal((p, k))
+        hx -= hx.mean(axis=1, keepdims=True)
+        rd = (1.0 / rng.uniform(0.5, 2.0, p) ** 2).astype(np.float32)
+        dep = rng.standard_normal(p)
+        rloc = rng.uniform(0.0, 1.0, p)
+        trans_o, wbar_o = orc.core(hx, rd, dep, rloc, 1.05)
+        t = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)  # noqa: E731
+        d = [t(hx), t(rd), t(dep), t(rloc)]
+        d_n = torch.tensor([p], dtype=torch.int32, device=dev)
+        d_off = torch.tensor([0], dtype=torch.int64, device=dev)
+        rel = {}
+        for prec in (lg.LG_PREC_MIXED, lg.LG_PREC_MIXED_TF32):
+            d_tr = torch.zeros((k, k), dtype=torch.float64, device=dev)
+            d_wb = torch.zeros(k, dtype=torch.float64, device=dev)
+            st = L.lg_core_batch(k, 1, ptr(d_n), ptr(d_off), *[ptr(x) for x in d], 1.05, prec,
+                                 ptr(d_tr), ptr(d_wb), None)
+            assert st == 0
+            torch.cuda.synchronize()
+            tr, wb = d_tr.cpu().numpy(), d_wb.cpu().numpy()
+            rel[prec] = (np.linalg.norm(tr - trans_o) / np.linalg.norm(trans_o),
+                         np.linalg.norm(wb - wbar_o) / max(np.linalg.norm(wbar_o), 1e-300))
+        r16, r32 = rel[lg.LG_PREC_MIXED], rel[lg.LG_PREC_MIXED_TF32]
+        assert r32[0] < 2e-6 and (p == 0 or r32[1] < 5e-6), (k, p, r32)
+        if p >= 300:
+            assert r32[0] < r16[0] / 2, (k, p, r16, r32)
+    # the TF32 Gram holds every member's hi and lo parts in one 128-row operand
+    d0 = torch.zeros(1, dtype=torch.int32, device=dev)
+    assert L.lg_core_batch(128, 1, ptr(d0), ptr(d0), None, None, None, None, 1.05,
+                           lg.LG_PREC_MIXED_TF32, ptr(d0), ptr(d0), None) == -3
+
+
+def test_tf32_analysis_within_1e4_and_closer_than_bf16():
+    import letkf_gb300 as lg
+    import synth
+    from oracle import oracle as orc
+
+    base = lg.preset("small3d")
+    w = synth.make_workload(base)
+    o = orc.Oracle(base, w.obs)
+    o.hx(w.xb, w.axb)
+    xa_o = np.zeros_like(w.xb)
+    axa_o = np.zeros_like(w.axb)
+    o.analysis(w.xb, w.axb, xa_o, axa_o)
+    errs = {}
+    for prec in (lg.LG_PREC_MIXED, lg.LG_PREC_MIXED_TF32):
+        cfg = base.replace(precision=prec)
+        ctx = lg.Letkf(cfg)
+        ctx.set_obs(w.obs)
+        xa = np.zeros_like(w.xb)
+        axa = np.zeros_like(w.axb)
+        ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+        assert ctx.stats()["n_gram_entries"] > 0
+        ctx.letkf_final()
+        errs[prec] = increment_rel_rms(cfg, w, (xa, axa), (xa_o, axa_o))
+    e16, e32 = errs[lg.LG_PREC_MIXED], errs[lg.LG_PREC_MIXED_TF32]
+    assert max(e32.values()) <= TOL_INCREMENT, e32
+    assert max(e32.values()) < max(e16.values()), (e16, e32)
+    with pytest.raises(RuntimeError, match="LG_ERR_UNSUPPORTED"):
+        lg.Letkf(base.replace(precision=lg.LG_PREC_MIXED_TF32, ens=128))
+
+
 @pytest.mark.parametrize("name", ["small3d", "tiny2d"])
 def test_tensor_core_gram_variants_agree(name, monkeypatch):
     """The column-group Gram (default), the per-solve streaming Gram and the

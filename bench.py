@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg3")
+    ap.add_argument("--ens", type=int, default=0, help="override the ensemble size")
     ap.add_argument("--precision", default=None, choices=[None, "fp64", "mixed", "tf32"])
     ap.add_argument("--no-tf32", action="store_true",
                     help="skip the TF32 (FP32-variant) Gram beside the BF16 one")
@@ -374,6 +375,8 @@ def main():
     lg_build.build()
 
     cfg = lg.preset(args.config)
+    if args.ens:
+        cfg = cfg.replace(ens=args.ens)
     if args.precision:
         cfg = cfg.replace(precision={"mixed": lg.LG_PREC_MIXED, "tf32": lg.LG_PREC_MIXED_TF32,
                                      "fp64": lg.LG_PREC_FP64}[args.precision])

@@ -1678,6 +1678,13 @@ int lg_run_device(lg_ctx* c, int ntimes, const double* xb, const double* axb, do
   return run_analysis(c, xb, axb, xa, axa, st, nullptr);
 }
 
+int lg_set_wait_limit(lg_ctx* c, int64_t ns) {
+  if (!c || ns < 0) return LG_ERR_ARG;
+  c->geo.tc_wait_ns = ns;
+  drop_graph(c);  // the limit is a kernel argument of the captured analysis
+  return LG_OK;
+}
+
 int lg_list_counts(lg_ctx* c, int* counts, int64_t* total) {
   if (!c || !counts) return LG_ERR_ARG;
   if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;

@@ -124,15 +124,17 @@ __device__ inline float gc_fast(float ri) {
   return 1.0f;
 }
 
-// Wait for a phase, suspending between polls; gives up after 2 s of wall time
-// (raising the CTA's abort flag) or as soon as another thread has given up.
-__device__ inline bool wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
+// Wait for a phase, suspending between polls; gives up after limit_ns of wall
+// time (2 s unless the context sets another, raising the CTA's abort flag) or
+// as soon as another thread has given up.
+__device__ inline bool wait(uint64_t* bar, uint32_t parity, volatile int* abort,
+                            unsigned long long limit_ns) {
   if (tc::mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = tc::global_ns();
   while (true) {
     if (tc::mbar_try_wait_hint(bar, parity, 1000u)) return true;
     if (*abort) return false;
-    if (tc::global_ns() - t0 > 2000000000ull) {
+    if (tc::global_ns() - t0 > limit_ns) {
       *abort = 1;
       return false;
     }
@@ -241,10 +243,12 @@ __global__ void __maxnreg__(128)
   tc::fence_after();
   const uint32_t tmem = tmem_base_sh;
 
+  const unsigned long long wait_ns =
+      g.tc_wait_ns > 0 ? (unsigned long long)g.tc_wait_ns : 2000000000ull;
   // lane 0 waits, the warp follows its outcome (keeps the warp converged)
   auto wait_warp = [&](uint64_t* bar, int parity) {
     int r = 0;
-    if (lane == 0) r = wait(bar, (uint32_t)(parity & 1), &s_abort) ? 1 : 0;
+    if (lane == 0) r = wait(bar, (uint32_t)(parity & 1), &s_abort, wait_ns) ? 1 : 0;
     return __shfl_sync(0xffffffffu, r, 0) != 0;
   };
   // the item's levels: lane lv (< G) holds level lv's ln p and record window;

@@ -30,6 +30,10 @@ struct Geometry {
   // QL sweep limit per eigenvalue (tql2 and dsyevd stop at 30-60 sweeps); 0 = 60.
   // A small value forces non-convergence (a host-side test of LG_ERR_EIG).
   int ql_max_iter;
+  // wall-clock limit of the column Gram's pipeline waits [ns]; 0 = 2 s.  A
+  // tiny value makes them run out (a host-side test of LG_ERR_TIMEOUT); the
+  // waits of a CTA's clean-up for its own MMAs and copies keep their full bound.
+  long long tc_wait_ns;
   // device arrays
   const float* glat;     // num_lat+1
   const float* glon;     // num_lon+1

@@ -366,6 +366,7 @@ def load_library(path: str = LIB_PATH):
     lib.lg_core_batch_noalloc.argtypes = lib.lg_core_batch.argtypes
     lib.lg_set_columns.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.lg_list_counts.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int64)]
+    lib.lg_set_wait_limit.argtypes = [C.c_void_p, C.c_int64]
     lib.lg_set_shard.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.lg_shard_entries.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64), P(C.c_int64)]
     lib.lg_hx_device.argtypes = [C.c_void_p] * 4
@@ -466,6 +467,10 @@ class Letkf:
     def set_columns(self, col_begin: int, col_end: int):
         """Analyse only columns [col_begin, col_end) (c = lon * num_lat + lat, 0-based)."""
         check(self.lib.lg_set_columns(self.h, col_begin, col_end), "lg_set_columns")
+
+    def set_wait_limit(self, ns: int):
+        """lg_set_wait_limit: the tensor-core Gram's wait limit in ns (0: 2 s)."""
+        check(self.lib.lg_set_wait_limit(self.h, ns), "lg_set_wait_limit")
 
     def list_counts(self) -> np.ndarray:
         """Local entries of every column's list (the count pass only)."""

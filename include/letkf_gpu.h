@@ -294,6 +294,14 @@ int lg_gmcore_to_da_device(int ens, int num_lat, int num_lon, int nz, int halo,
                            const double* d_pt, const double* d_area_subcell,
                            const double* d_area_cell, double* d_xb, void* stream);
 
+/* Wall-clock limit [ns] of the tensor-core Gram's pipeline waits (the column
+ * Gram's mbarrier waits between its producer, converter and MMA warps);
+ * 0 restores the default of 2 s.  On expiry a CTA raises LG_ERR_TIMEOUT,
+ * waits (with the full bound) for its own MMAs and copies, frees its tensor
+ * memory and returns, and the analysis returns LG_ERR_TIMEOUT.  For tests of
+ * that path and for diagnosing a stalled device; no reference counterpart. */
+int lg_set_wait_limit(lg_ctx* ctx, int64_t ns);
+
 /* Statistics of the last lg_run. */
 int lg_get_stats(const lg_ctx* ctx, lg_stats* st);
 

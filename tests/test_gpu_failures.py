@@ -101,6 +101,38 @@ def test_allocation_failure_reports_nomem_and_context_recovers(monkeypatch):
     ctx.letkf_final()
 
 
+def test_tensor_core_wait_limit_reports_timeout_and_context_recovers():
+    """A wait limit of 1 ns makes the column Gram's first pipeline wait run
+    out: its CTAs raise LG_ERR_TIMEOUT, wait (fully bounded) for their own MMAs
+    and copies, free their tensor memory and return, and the analysis returns
+    LG_ERR_TIMEOUT.  With the default limit back, the same context's next
+    analysis equals a fresh context's bit for bit."""
+    import letkf_gb300 as lg
+    import synth
+
+    cfg = lg.preset("small3d").replace(precision=lg.LG_PREC_MIXED, ens=64)
+    w = synth.make_workload(cfg)
+    ref = lg.Letkf(cfg)
+    ref.set_obs(w.obs)
+    xa_ref = np.zeros_like(w.xb)
+    axa_ref = np.zeros_like(w.axb)
+    ref.letkf_run(0, w.xb, w.axb, xa_ref, axa_ref)
+    ref.letkf_final()
+
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    ctx.set_tuning(gram_kernel=lg.LG_GRAM_COLUMN_LEAN)
+    xa = np.zeros_like(w.xb)
+    axa = np.zeros_like(w.axb)
+    ctx.set_wait_limit(1)
+    with pytest.raises(RuntimeError, match="LG_ERR_TIMEOUT"):
+        ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+    ctx.set_wait_limit(0)
+    ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+    assert np.array_equal(xa, xa_ref) and np.array_equal(axa, axa_ref)
+    ctx.letkf_final()
+
+
 def test_alloc_limit_in_the_batched_core(monkeypatch):
     import torch
     import letkf_gb300 as lg

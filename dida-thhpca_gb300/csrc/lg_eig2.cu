@@ -379,6 +379,185 @@ __global__ void __launch_bounds__(32) tridiag_kernel(int n, int nsolves, const d
   }
 }
 
+// Four warps per matrix, for 65..128 members.  With one warp per matrix the
+// packed triangle (up to 66 KB) leaves room for three CTAs, i.e. three warps,
+// per SM, and the FP64 pipe stays about a third busy (latency-bound); four
+// warps per matrix give twelve.  Same outputs as tridiag_kernel.  Each step's
+// scalars (square root, reflector norm, reciprocal) are computed once by
+// thread 0 and broadcast through shared memory, since an FP64 instruction
+// costs a full warp slot however few lanes it has; block sums are exact warp
+// sums combined by thread 0; the matrix-vector product splits the step's R
+// rows over groups of G lanes (G the largest power of two with R G <= 128,
+// at most 32), so it issues about R^2 / 32 FP64 instructions.
+constexpr int kTriWarps = 4;
+__global__ void __launch_bounds__(32 * kTriWarps) tridiag_mw_kernel(int n, int nsolves,
+                                                                   const double* Cin,
+                                                                   double* tri, int u32) {
+  constexpr int NT = 32 * kTriWarps;
+  const int s = blockIdx.x;
+  if (s >= nsolves) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  extern __shared__ double sm[];
+  __shared__ double s_part[kTriWarps];
+  __shared__ double s_res;
+  __shared__ double s_sc[3];  // inv_h, h, e_i of the step
+  const int np = n * (n + 1) / 2;
+  double* P = sm;      // packed lower triangle
+  double* q = P + np;  // n
+  const double* C = Cin + (size_t)s * n * n;
+  {
+    int j = 0, c = tid;
+    while (c > j) {
+      c -= j + 1;
+      ++j;
+    }
+    for (int t = tid; t < np; t += NT) {
+      P[t] = C[(size_t)j * n + c];
+      c += NT;
+      while (c > j) {
+        c -= j + 1;
+        ++j;
+      }
+    }
+  }
+  __syncthreads();
+  double* out = tri + (size_t)s * e2::tri_stride(n);
+  double* D = out;
+  double* E = out + n;
+  double* H = out + 2 * n;
+  double* U = out + 3 * n;
+  float* U32 = reinterpret_cast<float*>(U);
+  float* Act32 = U32 + (size_t)n * (n - 1) / 2;
+  // sum of one value per thread over the block: exact per warp, the four warp
+  // sums added by thread 0 in a fixed order; every thread gets the result
+  auto block_sum = [&](double v) -> double {
+    const double w = warp_sum_exact(v);
+    if (lane == 0) s_part[warp] = w;
+    __syncthreads();
+    if (tid == 0) s_res = (s_part[0] + s_part[1]) + (s_part[2] + s_part[3]);
+    __syncthreads();
+    return s_res;
+  };
+  bool extreme = false;
+  for (int i = n - 1; i >= 1; --i) {
+    const int l = i - 1;
+    double* row = P + tri_idx(i);
+    double h = 0.0, ei;
+    if (l > 0) {
+      double ss = 0.0;
+      for (int c = tid; c <= l; c += NT) ss = fma(row[c], row[c], ss);
+      double h0 = block_sum(ss);
+      double sc = 1.0;
+      bool scaled = false;
+      const int eh = dexp(h0);
+      if ((eh < 1023 - 900 || eh > 1023 + 900) && !is_zero_bits(h0)) {
+        double a1 = 0.0;
+        for (int c = tid; c <= l; c += NT) a1 += fabs(row[c]);
+        sc = block_sum(a1);
+        scaled = true;
+        const double inv = 1.0 / sc;
+        ss = 0.0;
+        for (int c = tid; c <= l; c += NT) {
+          const double v = row[c] * inv;
+          row[c] = v;
+          ss = fma(v, v, ss);
+        }
+        h0 = block_sum(ss);
+      }
+      if (is_zero_bits(h0)) {
+        ei = row[l];
+      } else {
+        if (tid == 0) {
+          const double f = row[l];
+          const double sq = sqrt(h0);
+          const double gg = nonneg_bits(f) ? neg_bits(sq) : sq;  // -sign(sqrt(h0), f)
+          s_sc[2] = scaled ? sc * gg : gg;
+          const double hh = h0 - f * gg;
+          s_sc[1] = hh;
+          s_sc[0] = rcp_nr(hh);
+          row[l] = f - gg;
+        }
+        __syncthreads();
+        const double inv_h = s_sc[0];
+        h = s_sc[1];
+        ei = s_sc[2];
+        // p = A u / h over the R = l + 1 rows, G lanes per row
+        const int R = l + 1;
+        int lf = 31 - __clz(NT / R);
+        lf = lf > 5 ? 5 : lf;
+        const int G = 1 << lf;
+        const int cl = (R + G - 1) >> lf;  // columns per lane
+        const int ri = tid >> lf, pi = tid & (G - 1);
+        const bool act = ri < R;
+        const int j = act ? ri : 0;
+        const int c0 = act ? min(R, pi * cl) : 0;
+        const int c1 = act ? min(R, c0 + cl) : 0;
+        const int tj = tri_idx(j);
+        double gj = 0.0;
+        int tcc = tri_idx(c0);
+        for (int c = c0; c < c1; ++c) {
+          const int off = (c <= j) ? tj + c : tcc + j;
+          gj = fma(P[off], row[c], gj);
+          tcc += c + 1;
+        }
+        if (G > 1) gj = group_sum_exact(gj, G);  // G is the same in every lane
+        double fs = 0.0;
+        if (act && pi == 0) {
+          const double pj = gj * inv_h;
+          q[j] = pj;
+          fs = pj * row[j];
+        }
+        // h lies in [2^-901, 2^902], so 1/h is normal and halving it is exact
+        const double kq = block_sum(fs) * half_bits(inv_h);
+        for (int jj = tid; jj <= l; jj += NT) q[jj] = fma(-kq, row[jj], q[jj]);
+        __syncthreads();
+        // A -= u q^T + q u^T over the packed rows 0..l
+        {
+          const int tot = tri_idx(l + 1);
+          int jr = 0, c = tid;
+          while (c > jr) {
+            c -= jr + 1;
+            ++jr;
+          }
+          for (int t = tid; t < tot; t += NT) {
+            P[t] = fma(-row[jr], q[c], fma(-q[jr], row[c], P[t]));
+            c += NT;
+            while (c > jr) {
+              c -= jr + 1;
+              ++jr;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    } else {
+      ei = row[l];
+    }
+    // reflector of step i: u = row i (scaled), h
+    if (u32) {
+      const int eh = dexp(h);
+      const bool in_range = eh >= 1023 - 200 && eh <= 1023 + 200;
+      extreme |= !is_zero_bits(h) && !in_range;
+      const float sv = in_range ? rsqrt_f32_of(h) : 0.0f;
+      for (int c = tid; c < i; c += NT) U32[e2::uoff(i) + c] = d2f_bits(row[c]) * sv;
+      if (tid == 0) Act32[i] = in_range ? 1.0f : 0.0f;
+    } else {
+      for (int c = tid; c < i; c += NT) U[e2::uoff(i) + c] = row[c];
+    }
+    if (tid == 0) {
+      H[i] = h;
+      E[i] = ei;
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += NT) D[i] = P[tri_idx(i) + i];
+  if (tid == 0) {
+    H[0] = extreme ? 1.0 : 0.0;
+    E[0] = 0.0;
+    if (u32) Act32[0] = 0.0f;
+  }
+}
+
 // ---------------------------------------------------------------- QL
 // lane-private arrays in shared memory are interleaved [index][lane]
 template <typename LT>
@@ -815,8 +994,16 @@ void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, cons
   // 1. tridiagonalisation
   if (phases & kEigTridiag) {
     const size_t smem_t = sizeof(double) * ((size_t)n * (n + 1) / 2 + n);
-    cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t);
-    tridiag_kernel<<<ns, 32, smem_t, stream>>>(n, ns, C, tri, sizeof(VT) == sizeof(float) ? 1 : 0);
+    const int u32 = sizeof(VT) == sizeof(float) ? 1 : 0;
+    if (n > 64) {  // four warps per matrix (up to 66 KB of triangle per CTA)
+      cudaFuncSetAttribute(tridiag_mw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem_t);
+      tridiag_mw_kernel<<<ns, 32 * kTriWarps, smem_t, stream>>>(n, ns, C, tri, u32);
+    } else {
+      cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem_t);
+      tridiag_kernel<<<ns, 32, smem_t, stream>>>(n, ns, C, tri, u32);
+    }
     if (ev_tri) record_event(ev_tri, stream);
   }
   if (phases & kEigQL) {

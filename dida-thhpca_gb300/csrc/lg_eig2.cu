@@ -28,6 +28,7 @@
 // holds, or (mixed path) whose reduction has an h beyond the FP32 reflector
 // range, is flagged and redone in FP64 by eig_apply_kernel (lg_eig.cu).
 #include <float.h>
+#include <stdlib.h>
 
 #include <algorithm>
 
@@ -995,7 +996,10 @@ void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, cons
   if (phases & kEigTridiag) {
     const size_t smem_t = sizeof(double) * ((size_t)n * (n + 1) / 2 + n);
     const int u32 = sizeof(VT) == sizeof(float) ? 1 : 0;
-    if (n > 64) {  // four warps per matrix (up to 66 KB of triangle per CTA)
+    // four warps per matrix above 64 members (up to 66 KB of triangle per
+    // CTA); LETKF_GB300_TRI_MW=1 takes them for every size (a diagnostic)
+    static const bool mw_all = getenv("LETKF_GB300_TRI_MW") != nullptr;
+    if (n > 64 || mw_all) {
       cudaFuncSetAttribute(tridiag_mw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem_t);
       tridiag_mw_kernel<<<ns, 32 * kTriWarps, smem_t, stream>>>(n, ns, C, tri, u32);

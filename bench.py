@@ -581,7 +581,12 @@ def main():
                    "columns": ncol, "solves_per_step": st["n_solves"],
                    "list_entries_per_step": st["nobsl_total"],
                    "gram_entries_per_step": iso["n_gram_entries"],
-                   "l2": "inputs (background 3.4 GB) larger than L2; no flush",
+                   "l2": "inputs (background %.1f GB) larger than L2; no flush" % (
+                       xb.numel() * 8 / 1e9),
+                   "column_windows": len(windows),
+                   "fresh_background": ("a fresh seeded perturbation ensemble before every "
+                                        "step (random orthogonal rotation of the members' "
+                                        "perturbations), untimed") if fresh else None,
                    "parallelism": (f"column shards over {world} GPUs (longitude blocks, one "
                                    f"H(x) all-gather per step)") if world > 1 else "single GPU",
                    "tuning": {kk: v for kk, v in tuning.items() if kk != "ms"}},

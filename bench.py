@@ -497,6 +497,27 @@ def main():
         ctx_v.letkf_final()
         variants["tf32"] = {"ms_per_step": ms_v, "value": ncol / (ms_v * 1e-3),
                             "ms_gram_last": st_v["ms_gram"], "xa": (xa_v, axa_v)}
+        # the BF16 Gram with the vector transform in FP64 (reflectors, rotation
+        # log and Xb.W from the FP64 eigensolve): the FP32 transform's share of
+        # the error and its time
+        os.environ["LETKF_GB300_VEC64"] = "1"
+        try:
+            ctx_w = lg.Letkf(cfg)
+        finally:
+            del os.environ["LETKF_GB300_VEC64"]
+        ctx_w.set_obs(w.obs)
+        xa_w, axa_w = torch.zeros_like(xa), torch.zeros_like(axa)
+        ctx_w.letkf_run_device(0, xb, axb, xa_w, axa_w, stream.cuda_stream)
+        torch.cuda.synchronize()
+        v0.record(stream)
+        for _ in range(args.variant_steps):
+            ctx_w.letkf_run_device(0, xb, axb, xa_w, axa_w, stream.cuda_stream)
+        v1.record(stream)
+        torch.cuda.synchronize()
+        ms_w = v0.elapsed_time(v1) / args.variant_steps
+        ctx_w.letkf_final()
+        variants["bf16_fp64_transform"] = {"ms_per_step": ms_w, "value": ncol / (ms_w * 1e-3),
+                                           "xa": (xa_w, axa_w)}
         variants["bf16"] = {"ms_per_step": ms, "value": value,
                             "xa": (xa_mixed, axa_mixed) if fp64_arm else None}
 
@@ -746,7 +767,9 @@ def main():
             name: {kk: v for kk, v in vd.items() if kk != "xa"} for name, vd in variants.items()}
         line["contraction_variants_note"] = (
             "the Gram contractions as BF16 hi/lo (the timed value) and as TF32 hi/lo tensor-core "
-            "products (the FP32 variant), same workload; errors against the plain-FP64 analysis")
+            "products (the FP32 variant), and the BF16 Gram with the vector transform (Xb.W, "
+            "w-bar) in FP64 instead of FP32; same workload; errors against the plain-FP64 "
+            "analysis")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ctx is not None:

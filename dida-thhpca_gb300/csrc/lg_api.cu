@@ -125,6 +125,11 @@ struct lg_ctx {
   double* d_trans = nullptr;
   size_t trans_cap = 0;
   bool use_eig2 = false;
+  // mixed precision: the vector transform (Xb.W, w-bar) in FP64 from FP64
+  // reflectors and rotations instead of FP32 (LETKF_GB300_VEC64=1 at
+  // lg_create; a diagnostic that isolates the FP32 transform's share of the
+  // mixed path's error)
+  bool vec64 = false;
   // analysed columns [col0, col1) (lg_set_columns / lg_set_shard; col1 < 0: all)
   // and the shard's own longitude blocks [shard_by0, shard_by1) (H(x) of
   // lg_hx_device: the copies of those blocks; shard_by1 < 0: every block)
@@ -497,6 +502,7 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   // localisation, whatever da_vert_distance is (letkf.F90:227-235)
   if (g.overlap > 0) c->cfg.vert_dist = 0.0;
   c->cubes = g.cube_n > 1 || g.overlap > 0 || (g.cube_nz > 1 && c->cfg.vert_dist > 0.0);
+  c->vec64 = getenv("LETKF_GB300_VEC64") != nullptr;
   cudaGetDevice(&c->dev);
   // Scheduling priorities of the solve streams (Gram, vector update, QL): a
   // level 0 (lowest, the default stream's), 1 or 2 (highest) each.  Pending
@@ -1151,7 +1157,7 @@ int prepare_capacity(lg_ctx* c) {
   const int nl = c->tune.solve_streams;
   // rotation log entries: (cos, sin) as two doubles, or two floats where only
   // the FP32 vector kernel replays them (mixed precision)
-  const size_t rot_pairs_per_slot = lg::mixed_precision(g.precision) ? 2 : 1;
+  const size_t rot_pairs_per_slot = lg::mixed_precision(g.precision) && !c->vec64 ? 2 : 1;
   for (int li = 0; li < 4; ++li) {
     lg_ctx::SolveLane& L = c->lane[li];
     const size_t cap = li < nl ? (size_t)c->chunk * levels : 0;
@@ -1441,7 +1447,7 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     if (nl >= 3) CK(cudaStreamWaitEvent(c->third_stream, c->ev_fork, 0));
     if (nl == 4) CK(cudaStreamWaitEvent(c->fourth_stream, c->ev_fork, 0));
   }
-  const bool fp32_vec = lg::mixed_precision(g.precision);
+  const bool fp32_vec = lg::mixed_precision(g.precision) && !c->vec64;
   for (int q = 0; q < nchunks; ++q) {
     const int set = q % nl;
     lg_ctx::SolveLane& L = c->lane[set];

@@ -232,6 +232,36 @@ def test_tf32_analysis_within_1e4():
         lg.Letkf(base.replace(precision=lg.LG_PREC_MIXED_TF32, ens=128))
 
 
+def test_mixed_gram_with_fp64_transform(monkeypatch):
+    """The BF16 Gram with the vector transform in FP64 (LETKF_GB300_VEC64, the
+    diagnostic that isolates the FP32 transform's share of the error): within
+    the bar, and no farther from the oracle than the default FP32 transform
+    plus a margin."""
+    import letkf_gb300 as lg
+    import synth
+    from oracle import oracle as orc
+
+    cfg = lg.preset("small3d").replace(precision=lg.LG_PREC_MIXED)
+    w = synth.make_workload(cfg)
+    o = orc.Oracle(cfg, w.obs)
+    o.hx(w.xb, w.axb)
+    xa_o = np.zeros_like(w.xb)
+    axa_o = np.zeros_like(w.axb)
+    o.analysis(w.xb, w.axb, xa_o, axa_o)
+    errs = {}
+    for vec64 in (False, True):
+        if vec64:
+            monkeypatch.setenv("LETKF_GB300_VEC64", "1")
+        ctx = lg.Letkf(cfg)
+        ctx.set_obs(w.obs)
+        xa = np.zeros_like(w.xb)
+        axa = np.zeros_like(w.axb)
+        ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+        ctx.letkf_final()
+        errs[vec64] = max(increment_rel_rms(cfg, w, (xa, axa), (xa_o, axa_o)).values())
+    assert errs[True] <= TOL_INCREMENT and errs[True] <= 1.5 * errs[False], errs
+
+
 @pytest.mark.parametrize("name", ["small3d", "tiny2d"])
 def test_tensor_core_gram_variants_agree(name, monkeypatch):
     """The column-group Gram (default), the per-solve streaming Gram and the

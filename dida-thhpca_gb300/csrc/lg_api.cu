@@ -1201,6 +1201,10 @@ int prepare_capacity(lg_ctx* c) {
 struct HostIO {
   const double *xb, *axb;
   double *xa, *axa;
+  // device addresses of xb and axb where the device can read them directly
+  // (mapped page-locked memory, 16-byte aligned sizes and addresses): the
+  // background then comes in by a copy kernel instead of the copy engine
+  const double *xb_map = nullptr, *axb_map = nullptr;
 };
 
 // Interior columns [c0, c1) of a [lon + 2 halo][lat + 2 halo][epc] array, device
@@ -1263,10 +1267,15 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
     const size_t cols = (size_t)(g.num_lat + 2 * g.halo) * (g.num_lon + 2 * g.halo);
     CK(cudaStreamWaitEvent(c->copy_stream, c->ev_fork, 0));
     CK(record_event(c->ev_io[0], c->copy_stream));
-    CK(cudaMemcpyAsync((void*)xb, io->xb, sizeof(double) * cols * c->geo.n * k,
-                       cudaMemcpyHostToDevice, c->copy_stream));
-    CK(cudaMemcpyAsync((void*)axb, io->axb, sizeof(double) * cols * c->geo.n,
-                       cudaMemcpyHostToDevice, c->copy_stream));
+    const size_t bx = sizeof(double) * cols * c->geo.n * k, ba = sizeof(double) * cols * c->geo.n;
+    if (io->xb_map && io->axb_map) {
+      CK(lg::launch_copy_mapped(io->xb_map, (void*)xb, bx, c->copy_stream));
+      CK(lg::launch_copy_mapped(io->axb_map, (void*)axb, ba, c->copy_stream));
+      launches += 2;
+    } else {
+      CK(cudaMemcpyAsync((void*)xb, io->xb, bx, cudaMemcpyHostToDevice, c->copy_stream));
+      CK(cudaMemcpyAsync((void*)axb, io->axb, ba, cudaMemcpyHostToDevice, c->copy_stream));
+    }
     CK(record_event(c->ev_io[1], c->copy_stream));
     CK(cudaEventRecord(c->ev_copy_in, c->copy_stream));
     CK(cudaStreamWaitEvent(c->side_stream, c->ev_copy_in, 0));
@@ -1576,7 +1585,8 @@ int run_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, dou
                          io ? io->xa : nullptr, io ? io->axa : nullptr,
                          (const void*)(intptr_t)c->col0, (const void*)(intptr_t)c->col1,
                          (const void*)(intptr_t)(phases | (own_copies ? 4 : 0) |
-                                                 (c->shard_by0 << 3) | ((c->shard_by1 + 1) << 16))};
+                                                 (c->shard_by0 << 3) | ((c->shard_by1 + 1) << 16) |
+                                                 ((io && io->xb_map) ? (1 << 30) : 0))};
   bool ran = false;
   if (graphs) {
     cudaGraphExec_t& gx = c->graph_exec[phases];
@@ -1672,6 +1682,21 @@ bool pinned(const void* p) {
     return false;
   }
   return a.type == cudaMemoryTypeHost;
+}
+
+// the device address of page-locked host memory p of `bytes` bytes, when the
+// device can read it directly and address and size are 16-byte multiples;
+// nullptr otherwise (LETKF_GB300_COPY_ENGINE=1 always gives nullptr)
+const double* mapped(const void* p, size_t bytes) {
+  if (getenv("LETKF_GB300_COPY_ENGINE")) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
+  if (((uintptr_t)a.devicePointer | bytes) % 16 != 0) return nullptr;
+  return static_cast<const double*>(a.devicePointer);
 }
 }  // namespace
 
@@ -1825,7 +1850,9 @@ int lg_run(lg_ctx* c, int ntimes, const double* xb, const double* axb, double* x
   cudaStream_t st = c->own_stream;
   if (pinned(xb) && pinned(axb) && pinned(xa) && pinned(axa)) {
     // page-locked host arrays: the copies run inside the analysis, overlapped
-    const HostIO io{xb, axb, xa, axa};
+    HostIO io{xb, axb, xa, axa};
+    io.xb_map = mapped(xb, sizeof(double) * cols * n * k);
+    io.axb_map = mapped(axb, sizeof(double) * cols * n);
     return run_analysis(c, c->d_xb, c->d_axb, c->d_xa, c->d_axa, st, &io);
   }
   CK(cudaEventRecord(c->ev_io[0], st));

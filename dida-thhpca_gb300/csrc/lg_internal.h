@@ -269,5 +269,8 @@ void launch_post(int ens, int n, int num_lat, int num_lon, int halo, double gamm
                  const double* xa, const double* axa, double* xa_out, double* spread_b,
                  double* spread_a, cudaStream_t stream);
 void launch_nan_check(const double* x, size_t n, int* err, cudaStream_t stream);
+// bytes (a multiple of 16) from device-addressable page-locked host memory src
+// (16-byte aligned) to device memory dst (16-byte aligned), by a copy kernel
+cudaError_t launch_copy_mapped(const void* src, void* dst, size_t bytes, cudaStream_t stream);
 
 }  // namespace lg

@@ -105,18 +105,22 @@ def test_autotune_mixed_keeps_the_increment_within_tolerance():
     ctx.letkf_final()
 
 
-@pytest.mark.parametrize("mb1", [False, True])
-def test_host_run_pinned_overlapped_copies_match_pageable(mb1, monkeypatch):
+@pytest.mark.parametrize("mb1,engine", [(False, False), (True, False), (False, True)])
+def test_host_run_pinned_overlapped_copies_match_pageable(mb1, engine, monkeypatch):
     """lg_run with page-locked host arrays copies the background in beside the
-    selection and each chunk's columns out beside the later chunks; the result
-    is bit-identical to the pageable-array path (copies before and after), and
-    the halo of the host arrays is left untouched.  1 MiB chunks split
-    longitude rows, exercising the partial-row copies."""
+    selection (by a copy kernel reading the mapped host memory, or with
+    LETKF_GB300_COPY_ENGINE by the copy engine) and each chunk's columns out
+    beside the later chunks; the result is bit-identical to the pageable-array
+    path (copies before and after), and the halo of the host arrays is left
+    untouched.  1 MiB chunks split longitude rows, exercising the partial-row
+    copies."""
     import torch
 
     import letkf_gb300 as lg
     if mb1:
         monkeypatch.setenv("LETKF_GB300_CHUNK_MB", "1")
+    if engine:
+        monkeypatch.setenv("LETKF_GB300_COPY_ENGINE", "1")
     for prec in (lg.LG_PREC_FP64, lg.LG_PREC_MIXED):
         cfg, w = _workload("tiny3d", precision=prec)
         ctx = lg.Letkf(cfg)

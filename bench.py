@@ -72,7 +72,7 @@ def parse():
                     help="skip the TF32 (FP32-variant) Gram beside the BF16 one")
     ap.add_argument("--variant-steps", type=int, default=3,
                     help="timed analyses of the TF32 variant (after one untimed one)")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the bounded oracle sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -187,6 +187,18 @@ def fp64_peak_tflops(torch, dev):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def workload_config(cfg):
+    """The `config` object of both arms' lines: the workload, by its shape."""
+    return {"workload": f"{cfg.name}: {cfg.num_lon}x{cfg.num_lat}x{cfg.nz}, "
+                        f"{'/'.join(cfg.var_names)}, N={cfg.ens}, {cfg.n_obs} obs"
+                        + (f" ({int(100 * cfg.clustered_frac)}% clustered)"
+                           if cfg.clustered_frac else "")
+                        + f", L={cfg.local_dist:g} km, vert {cfg.vert_dist:g} ln p, "
+                          f"rho={cfg.inflation}",
+            "columns": cfg.num_lat * cfg.num_lon,
+            "l2": "inputs larger than L2; no flush between steps"}
+
+
 def spread_order(cfg, seed=0, n_bands=12, n_sectors=16):
     """All grid columns in an order whose every prefix is spread over the
     globe: rounds of one seeded random column from each of n_bands latitude
@@ -313,8 +325,8 @@ def reference_arm(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cfg.num_lat * cfg.num_lon / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded spherical-harmonic ensemble, uniform observations)",
-        "config": {"workload": f"{cfg.name}: {cfg.num_lon}x{cfg.num_lat}x{cfg.nz}, N={cfg.ens}, "
-                               f"{cfg.n_obs} obs, L={cfg.local_dist:g} km"},
+        "config": workload_config(cfg),
+        "run": {"precision": "fp64 (the reference's own arithmetic)", "threads": nthreads},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": info["sample"], "sample_columns": info["sample_columns"],
                          "sample_seconds": info["sample_seconds"],
@@ -594,12 +606,10 @@ def main():
         "data": "synthetic (seeded spherical-harmonic ensemble, %s observations)" % (
             "uniform" if not cfg.clustered_frac else
             f"{int(100 * cfg.clustered_frac)}% clustered + uniform"),
-        "config": {"workload": f"{cfg.name}: {cfg.num_lon}x{cfg.num_lat}x{cfg.nz}, ps/u/v/pt, "
-                               f"N={cfg.ens}, {cfg.n_obs} obs, L={cfg.local_dist:g} km, "
-                               f"vert {cfg.vert_dist:g} ln p, rho={cfg.inflation}",
-                   "precision": {lg.LG_PREC_MIXED: "mixed", lg.LG_PREC_MIXED_TF32: "mixed-tf32",
-                                 lg.LG_PREC_FP64: "fp64"}[cfg.precision],
-                   "columns": ncol, "solves_per_step": st["n_solves"],
+        "config": workload_config(cfg),
+        "run": {"precision": {lg.LG_PREC_MIXED: "mixed", lg.LG_PREC_MIXED_TF32: "mixed-tf32",
+                              lg.LG_PREC_FP64: "fp64"}[cfg.precision],
+                   "solves_per_step": st["n_solves"],
                    "list_entries_per_step": st["nobsl_total"],
                    "gram_entries_per_step": iso["n_gram_entries"],
                    "l2": "inputs (background %.1f GB) larger than L2; no flush" % (

@@ -1748,6 +1748,7 @@ int lg_list_counts(lg_ctx* c, int* counts, int64_t* total) {
     *total = t;
   }
   c->capacity_ready = false;  // the next analysis recounts its own columns
+  drop_graph(c);              // and recaptures against whatever it sizes
   return LG_OK;
 }
 

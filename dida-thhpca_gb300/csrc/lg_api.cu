@@ -1908,6 +1908,8 @@ int lg_run_da_parallel(lg_ctx* c, int ntimes, double gamma1, double gamma2, doub
                        const double* xb_in, double* xa_out, double* spread_b, double* spread_a) {
   if (!c || !xb_in || !xa_out || !spread_b || !spread_a) return LG_ERR_ARG;
   if (!c->have_grid || !c->have_obs) return LG_ERR_STATE;
+  // the blend and spreads cover the whole globe: not with a column window or shard
+  if (windowed(c)) return LG_ERR_UNSUPPORTED;
   const lg_config& g = c->cfg;
   const size_t cols = (size_t)(g.num_lat + 2 * g.halo) * (g.num_lon + 2 * g.halo);
   const size_t n = c->geo.n, k = g.ens;

@@ -246,7 +246,8 @@ int lg_post_device(lg_ctx* ctx, double gamma1, double gamma2, double polar_lat,
                    double* d_spread_a, void* stream);
 
 /* run_da_parallel as a whole on host arrays (module_da_parallel.F90:165-263):
- * split, letkf_run, blend and spreads.  xb_in/xa_out have the xb layout. */
+ * split, letkf_run, blend and spreads.  xb_in/xa_out have the xb layout.
+ * Whole globe only: LG_ERR_UNSUPPORTED while a column window or shard is set. */
 int lg_run_da_parallel(lg_ctx* ctx, int ntimes, double gamma1, double gamma2, double polar_lat,
                        const double* xb_in, double* xa_out, double* spread_b,
                        double* spread_a);

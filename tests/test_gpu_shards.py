@@ -166,4 +166,14 @@ def test_window_arguments_validated():
             ctx.set_columns(a, b)
     with pytest.raises(RuntimeError, match="LG_ERR_ARG"):
         ctx.set_shard(0, cfg.global_ny + 1)
+    # run_da_parallel post-processes the whole globe: refused with a window set
+    import synth
+    w = synth.make_workload(cfg)
+    ctx.set_obs(w.obs)
+    ctx.set_columns(0, cfg.num_lat)
+    full = np.ascontiguousarray(w.xb + w.axb[..., None])
+    out = np.zeros_like(full)
+    sp = np.zeros((cfg.num_lon, cfg.num_lat, cfg.n_rows))
+    with pytest.raises(RuntimeError, match="LG_ERR_UNSUPPORTED"):
+        ctx.run_da_parallel(0, 0.0, 1.0, 90.0, full, out, sp, sp.copy())
     ctx.letkf_final()

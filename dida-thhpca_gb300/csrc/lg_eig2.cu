@@ -637,15 +637,19 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
       g = DD(m) - DD(l) + EE(l) / (g + (g >= 0.0 ? r : -r));
       double sn = 1.0, cn = 1.0, p = 0.0;
       bool early = false;
+      // d[i + 1] of the next rotation is the d[i] this one reads (a rotation
+      // writes only d[i + 1] and e[i + 1]): carried in a register, not reloaded
+      double d_hi = DD(m);
       for (int i = m - 1; i >= l; --i) {
         const double ei = EE(i);
+        const double d_lo = DD(i);
         const double f = sn * ei, b = cn * ei;
         const double q2 = f * f + g * g;
         // q2 == 0 on the bit pattern (off the FP64 pipe): a sum of squares is
         // never -0, and a NaN is not zero either way
         if ((__double2hiint(q2) | __double2loint(q2)) == 0) {
           EE(i + 1) = 0.0;
-          DD(i + 1) -= p;
+          DD(i + 1) = d_hi - p;
           EE(m) = 0.0;
           early = true;
           break;
@@ -656,10 +660,11 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
         EE(i + 1) = r;
         sn = f * rinv;
         cn = g * rinv;
-        g = DD(i + 1) - p;
-        r = (DD(i) - g) * sn + 2.0 * cn * b;
+        g = d_hi - p;
+        r = (d_lo - g) * sn + 2.0 * cn * b;
         p = sn * r;
         DD(i + 1) = g + p;
+        d_hi = d_lo;
         g = cn * r - b;
         if (nrot < rot_cap) {
           cs_log[nrot] = make_rot<LT>(cn, sn);

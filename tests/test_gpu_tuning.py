@@ -144,6 +144,36 @@ def test_host_run_pinned_overlapped_copies_match_pageable(mb1, engine, monkeypat
         ctx.letkf_final()
 
 
+def test_pinned_arrays_off_16_byte_alignment_use_the_copy_engine():
+    """Page-locked host arrays whose address is not a multiple of 16 bytes
+    cannot be read by the 16-byte loads of the copy kernel: lg_run copies them
+    with the copy engine instead, with the same result."""
+    import torch
+
+    import letkf_gb300 as lg
+    cfg, w = _workload("tiny3d", precision=lg.LG_PREC_MIXED)
+    ctx = lg.Letkf(cfg)
+    ctx.set_obs(w.obs)
+    xa = np.zeros_like(w.xb)
+    axa = np.zeros_like(w.axb)
+    ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+
+    def pinned_off8(a):
+        buf = torch.empty(a.size + 1, dtype=torch.float64, pin_memory=True)
+        v = buf.numpy()[1:].reshape(a.shape)  # 8 bytes past a 16-byte boundary
+        assert v.ctypes.data % 16 == 8
+        v[...] = a
+        return v
+
+    pxb, paxb = pinned_off8(w.xb), pinned_off8(w.axb)
+    pxa, paxa = pinned_off8(np.zeros_like(w.xb)), pinned_off8(np.zeros_like(w.axb))
+    ctx.letkf_run(0, pxb, paxb, pxa, paxa)
+    h = cfg.halo
+    assert np.array_equal(pxa[h:-h, h:-h], xa[h:-h, h:-h])
+    assert np.array_equal(paxa[h:-h, h:-h], axa[h:-h, h:-h])
+    ctx.letkf_final()
+
+
 def test_observation_sets_of_changing_size_reuse_buffers():
     """One context through a small, a larger and the small observation set
     again (buffers kept across sets, grown when outgrown) gives the same

@@ -314,15 +314,22 @@ def reference_arm(args):
     vals = []
     info = {}
     xb_h, axb_h = np.ascontiguousarray(w.xb), np.ascontiguousarray(w.axb)
+    step_s = []
     for i in range(args.warmup + args.steps):
         # each step its own globe-spread sample (seed = step index)
+        t0 = time.perf_counter()
         v, info = cpu_sample(cfg, w.obs, xb_h, axb_h, per_step, nthreads, seed=i)
         if i >= args.warmup:
             vals.append(v)
+            step_s.append(time.perf_counter() - t0)
     value = statistics.median(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cfg.num_lat * cfg.num_lon / value,
+        "steps": args.steps, "warmup": args.warmup,
+        # a step is one bounded sample (its wall time); the full analysis at
+        # the sampled rate is extrapolated separately
+        "ms_per_step": 1e3 * statistics.median(step_s),
+        "ms_per_full_analysis_extrapolated": 1e3 * cfg.num_lat * cfg.num_lon / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded spherical-harmonic ensemble, uniform observations)",
         "config": workload_config(cfg),

@@ -1105,6 +1105,9 @@ int prepare_capacity(lg_ctx* c) {
   c->rot_cap = 3 * k * k;
   // test hook: a small log forces the overflow fallback path
   if (const char* env = getenv("LETKF_GB300_ROT_CAP")) c->rot_cap = std::max(1, atoi(env));
+  // a multiple of 8 entries: the vector kernel reads each solve's log in
+  // aligned groups of eight
+  c->rot_cap = (c->rot_cap + 7) & ~7;
   if (c->cubes) {
     // cube solves: one buffer set of Gram matrices for a chunk of solves, and
     // every solve's trans (the columns of a cube may take it from several)

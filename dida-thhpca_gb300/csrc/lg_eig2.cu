@@ -87,6 +87,23 @@ __device__ inline double neg_bits(double x) {
 __device__ inline double half_bits(double x) {
   return __hiloint2double(__double2hiint(x) - (1 << 20), __double2loint(x));
 }
+// 2 x for every double x, exactly as the FP64 pipe rounds it: a subnormal's
+// magnitude bits shift left by one (carrying into the exponent where the
+// result is normal), a normal's exponent goes up by one, the largest binade
+// overflows to infinity, and zero, infinity and NaN stay as they are.
+__device__ inline double twice_bits(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long sign = u & 0x8000000000000000ull;
+  unsigned long long mag = u ^ sign;
+  const unsigned e = (unsigned)(mag >> 52);
+  if (e == 0u)
+    mag <<= 1;
+  else if (e < 2046u)
+    mag += 1ull << 52;
+  else if (e == 2046u)
+    mag = 0x7ff0000000000000ull;
+  return __longlong_as_double((long long)(sign | mag));
+}
 
 // Sum of one finite double per lane over the warp, on the integer pipe: each
 // value is aligned at the warp's largest exponent into a signed 128-bit fixed
@@ -632,7 +649,7 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
     }
     if (__all_sync(0xffffffffu, done)) break;
     if (!done) {
-      double g = (DD(l + 1) - DD(l)) / (2.0 * EE(l));
+      double g = (DD(l + 1) - DD(l)) / twice_bits(EE(l));
       double r = sqrt(g * g + 1.0);
       g = DD(m) - DD(l) + EE(l) / (g + (g >= 0.0 ? r : -r));
       double sn = 1.0, cn = 1.0, p = 0.0;
@@ -661,7 +678,7 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
         sn = f * rinv;
         cn = g * rinv;
         g = d_hi - p;
-        r = (d_lo - g) * sn + 2.0 * cn * b;
+        r = (d_lo - g) * sn + twice_bits(cn) * b;  // 2 cn off the FP64 pipe
         p = sn * r;
         DD(i + 1) = g + p;
         d_hi = d_lo;
@@ -702,11 +719,114 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
 }
 
 // ---------------------------------------------------------------- vectors + update
+// Streaming reads of the rotation log and the reflectors.  Both were written by
+// an earlier launch and, at the full sizes, are no longer in L2 when the vector
+// kernel reads them (a chunk's logs are about a gigabyte).  A lane replays its
+// rotations one after another, each depending on the previous through the
+// vector, so one load per rotation would leave the chain waiting on DRAM at
+// every step.  The log is therefore read kRotBatch entries at a time, one batch
+// ahead of the rotations that use it (the loads of a batch are independent and
+// in flight together), and every load asks L2 for the whole 256-byte segment
+// around it, so that the following entries are found there.  The data are
+// read-only for the kernel (non-coherent loads).
+constexpr int kRotBatch = 8;
+
+template <typename LT>
+__device__ inline LT ld_stream(const LT* p);
+template <>
+__device__ inline float2 ld_stream<float2>(const float2* p) {
+  float2 v;
+  asm("ld.global.nc.L2::256B.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+  return v;
+}
+template <>
+__device__ inline double2 ld_stream<double2>(const double2* p) {
+  double2 v;
+  asm("ld.global.nc.L2::256B.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+  return v;
+}
+template <>
+__device__ inline float ld_stream<float>(const float* p) {
+  float v;
+  asm("ld.global.nc.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+template <>
+__device__ inline double ld_stream<double>(const double* p) {
+  double v;
+  asm("ld.global.nc.L2::256B.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
+// One bulk prefetch into L2 of the 16-byte-aligned interior of [p, p + bytes):
+// a solve's reflector block, just before a Householder pass reads it step by
+// step (each step's loads would otherwise wait on DRAM in turn).
+__device__ inline void prefetch_l2(const void* p, size_t bytes) {
+  const size_t a0 = __cvta_generic_to_global(p);
+  const size_t a = (a0 + 15) & ~(size_t)15, e = (a0 + bytes) & ~(size_t)15;
+  if (e > a)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(e - a))
+                 : "memory");
+}
+
+// Steps of the reduction that have a reflector (FP32 flags of the mixed path),
+// read once as a bit mask for up to 128 members; the flag loads are
+// independent, so they wait on memory once instead of once per step.
+struct StepMask {
+  unsigned long long lo = 0, hi = 0;
+  __device__ bool has(int i) const { return ((i < 64 ? lo >> i : hi >> (i - 64)) & 1ull) != 0; }
+};
+__device__ inline StepMask load_step_mask(const float* act, int n) {
+  StepMask m;
+  for (int i = 1; i < n; ++i) {
+    if (ld_stream(act + i) != 0.0f) {
+      if (i < 64)
+        m.lo |= 1ull << i;
+      else
+        m.hi |= 1ull << (i - 64);
+    }
+  }
+  return m;
+}
+
+// Eight consecutive log entries 8b .. 8b + 7 (the log of a solve starts on a
+// 64-byte boundary and its capacity is a multiple of 8, so these loads are
+// aligned vector loads inside the solve's log; entries past the solve's count
+// are read but never used).
+template <typename LT>
+struct RotBatch {
+  LT cs[kRotBatch];
+  uint2 ix;  // eight one-byte indices
+  __device__ int idx(int j) const { return (int)(((j < 4 ? ix.x : ix.y) >> (8 * (j & 3))) & 0xffu); }
+};
+
+template <typename LT>
+__device__ inline void load_rot_batch(RotBatch<LT>& rb, const LT* cs, const unsigned char* ix,
+                                      int b) {
+  const size_t r0 = (size_t)b * kRotBatch;
+  if constexpr (sizeof(LT) == sizeof(float2)) {
+    const float4* p = reinterpret_cast<const float4*>(cs + r0);
+#pragma unroll
+    for (int j = 0; j < kRotBatch / 2; ++j) {
+      float4 v;
+      asm("ld.global.nc.L2::256B.v4.f32 {%0, %1, %2, %3}, [%4];"
+          : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+          : "l"(p + j));
+      rb.cs[2 * j] = LT{v.x, v.y};
+      rb.cs[2 * j + 1] = LT{v.z, v.w};
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kRotBatch; ++j) rb.cs[j] = ld_stream(cs + r0 + j);
+  }
+  asm("ld.global.nc.L2::256B.v2.u32 {%0, %1}, [%2];" : "=r"(rb.ix.x), "=r"(rb.ix.y) : "l"(ix + r0));
+}
+
 // lanes: solve-slot q = lane / per, vector v = lane % per (v = 0: t, v >= 1: row v-1)
 // VT: arithmetic of the vector transforms (double: FP64 path; float: the mixed
 // path's Xb.W contraction, with eigenvalues, rotations and reflectors from FP64)
 template <typename VT, typename LT>
-__global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, const double* tin,
+__global__ void __launch_bounds__(256) __maxnreg__(sizeof(VT) == sizeof(float) ? 72 : 128) vec_kernel(Geometry g, SolveBatch b, const double* tin,
                                                   const double* tri, const double* lam,
                                                   const LT* rot_cs,
                                                   const unsigned char* rot_i, const int* rot_n,
@@ -735,6 +855,14 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
   // per-slot t_j / lambda_j, shared by the row lanes of the slot
   VT* tslot = sm + (size_t)warps * 32 * n + (size_t)w * slots * n;
 #define YY(i) y[(i) * 32 + lane]
+  // y <- y - u (u . y) / h over the first i entries (the FP32 reflectors are
+  // normalised: no division)
+  auto reflect = [&](const auto* u, int i, bool div, double h) {
+    VT dot = 0;
+    for (int kk = 0; kk < i; ++kk) dot += (VT)u[kk] * YY(kk);
+    if (div) dot /= (VT)h;
+    for (int kk = 0; kk < i; ++kk) YY(kk) -= (VT)u[kk] * dot;
+  };
   const bool active = (lane < slots * per) && (s < b.nsolves);
   int r_state = -1;  // state row of this lane
   size_t ci = 0;
@@ -775,35 +903,41 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
     if constexpr (kF32) {
       const float* U32 = reinterpret_cast<const float*>(T + 3 * n);
       const float* Act32 = U32 + (size_t)n * (n - 1) / 2;
+      prefetch_l2(U32, sizeof(float) * ((size_t)n * (n - 1) / 2 + n));
+      const StepMask act = load_step_mask(Act32, n);
       for (int i = n - 1; i >= 1; --i) {
-        if (Act32[i] == 0.0f) continue;
-        const float* u = U32 + e2::uoff(i);  // v = u / sqrt(h): P = I - v v^T
-        float dot = 0.0f;
-        for (int kk = 0; kk < i; ++kk) dot += u[kk] * YY(kk);
-        for (int kk = 0; kk < i; ++kk) YY(kk) -= u[kk] * dot;
+        if (!act.has(i)) continue;
+        reflect(U32 + e2::uoff(i), i, false, 1.0);  // v = u / sqrt(h): P = I - v v^T
       }
     } else {
       const double* H = T + 2 * n;
       const double* U = T + 3 * n;
+      prefetch_l2(H, sizeof(double) * ((size_t)n + (size_t)n * (n - 1) / 2));
       for (int i = n - 1; i >= 1; --i) {
         const double h = H[i];
         if (h == 0.0) continue;
-        const double* u = U + e2::uoff(i);
-        VT dot = 0;
-        for (int kk = 0; kk < i; ++kk) dot += (VT)u[kk] * YY(kk);
-        dot /= (VT)h;
-        for (int kk = 0; kk < i; ++kk) YY(kk) -= (VT)u[kk] * dot;
+        reflect(U + e2::uoff(i), i, true, h);
       }
     }
     // y = Z^T y: rotations in generation order
     const LT* cs = rot_cs + (size_t)s * rot_cap;
     const unsigned char* ix = rot_i + (size_t)s * rot_cap;
-    for (int r = 0; r < nrot; ++r) {
-      const LT c = cs[r];
-      const int i = ix[r];
-      const VT a0 = YY(i), a1 = YY(i + 1);
-      YY(i) = (VT)c.x * a0 - (VT)c.y * a1;
-      YY(i + 1) = (VT)c.y * a0 + (VT)c.x * a1;
+    const int nb = (nrot + kRotBatch - 1) / kRotBatch;
+    RotBatch<LT> cur, nxt;
+    if (nb > 0) load_rot_batch(cur, cs, ix, 0);
+    for (int bb = 0; bb < nb; ++bb) {
+      if (bb + 1 < nb) load_rot_batch(nxt, cs, ix, bb + 1);
+#pragma unroll
+      for (int j = 0; j < kRotBatch; ++j) {
+        if (bb * kRotBatch + j < nrot) {
+          const LT c = cur.cs[j];
+          const int i = cur.idx(j);
+          const VT a0 = YY(i), a1 = YY(i + 1);
+          YY(i) = (VT)c.x * a0 - (VT)c.y * a1;
+          YY(i + 1) = (VT)c.y * a0 + (VT)c.x * a1;
+        }
+      }
+      cur = nxt;
     }
     if (v == 0) {
       VT* ts = tslot + (size_t)q * n;
@@ -839,35 +973,41 @@ __global__ void __launch_bounds__(256) vec_kernel(Geometry g, SolveBatch b, cons
     // y = Z y: rotations in reverse order
     const LT* cs = rot_cs + (size_t)s * rot_cap;
     const unsigned char* ix = rot_i + (size_t)s * rot_cap;
-    for (int r = nrot - 1; r >= 0; --r) {
-      const LT c = cs[r];
-      const int i = ix[r];
-      const VT a0 = YY(i), a1 = YY(i + 1);
-      YY(i) = (VT)c.x * a0 + (VT)c.y * a1;
-      YY(i + 1) = -(VT)c.y * a0 + (VT)c.x * a1;
+    const int nb = (nrot + kRotBatch - 1) / kRotBatch;
+    RotBatch<LT> cur, nxt;
+    if (nb > 0) load_rot_batch(cur, cs, ix, nb - 1);
+    for (int bb = nb - 1; bb >= 0; --bb) {
+      if (bb > 0) load_rot_batch(nxt, cs, ix, bb - 1);
+#pragma unroll
+      for (int j = kRotBatch - 1; j >= 0; --j) {
+        if (bb * kRotBatch + j < nrot) {
+          const LT c = cur.cs[j];
+          const int i = cur.idx(j);
+          const VT a0 = YY(i), a1 = YY(i + 1);
+          YY(i) = (VT)c.x * a0 + (VT)c.y * a1;
+          YY(i + 1) = -(VT)c.y * a0 + (VT)c.x * a1;
+        }
+      }
+      cur = nxt;
     }
     // y = Q y = P_{n-1} ... P_1 y  (P_1 first)
     if constexpr (kF32) {
       const float* U32 = reinterpret_cast<const float*>(T + 3 * n);
       const float* Act32 = U32 + (size_t)n * (n - 1) / 2;
+      prefetch_l2(U32, sizeof(float) * ((size_t)n * (n - 1) / 2 + n));
+      const StepMask act = load_step_mask(Act32, n);
       for (int i = 1; i < n; ++i) {
-        if (Act32[i] == 0.0f) continue;
-        const float* u = U32 + e2::uoff(i);
-        float dot = 0.0f;
-        for (int kk = 0; kk < i; ++kk) dot += u[kk] * YY(kk);
-        for (int kk = 0; kk < i; ++kk) YY(kk) -= u[kk] * dot;
+        if (!act.has(i)) continue;
+        reflect(U32 + e2::uoff(i), i, false, 1.0);
       }
     } else {
       const double* H = T + 2 * n;
       const double* U = T + 3 * n;
+      prefetch_l2(H, sizeof(double) * ((size_t)n + (size_t)n * (n - 1) / 2));
       for (int i = 1; i < n; ++i) {
         const double h = H[i];
         if (h == 0.0) continue;
-        const double* u = U + e2::uoff(i);
-        VT dot = 0;
-        for (int kk = 0; kk < i; ++kk) dot += (VT)u[kk] * YY(kk);
-        dot /= (VT)h;
-        for (int kk = 0; kk < i; ++kk) YY(kk) -= (VT)u[kk] * dot;
+        reflect(U + e2::uoff(i), i, true, h);
       }
     }
     // xa = axb + sqrt(rho) x + (W - sqrt(rho) I) x + overline_w . x, recentred

@@ -378,9 +378,11 @@ __global__ void __maxnreg__(128)
       item_windows(item, col, kk0, G, al, w0, w1, u0, u1);
       const int nst = u1 > u0 ? (u1 - u0 + kRows - 1) / kRows : 0;
       unsigned started = 0u;
-      float tacc[kG];
+      // t of each level as two FP32 partial sums (even and odd records) in one
+      // packed register, added at the end
+      unsigned long long tacc[kG];
 #pragma unroll
-      for (int lv = 0; lv < kG; ++lv) tacc[lv] = 0.0f;
+      for (int lv = 0; lv < kG; ++lv) tacc[lv] = 0ull;
       bool ok = true;
       // Every converter warp runs all nst stages and reaches every quarter
       // barrier, also after a failed wait (then it only skips the work), so the
@@ -452,11 +454,11 @@ __global__ void __maxnreg__(128)
             uint32_t hi[4], lo[4];
 #pragma unroll
             for (int jj = 0; jj < 8; jj += 2) {
-              const float v0 = y[h * 8 + jj] * swv[jj];
-              const float v1 = y[h * 8 + jj + 1] * swv[jj + 1];
-              tacc[lv] = fmaf(v0, sdv[jj], tacc[lv]);
-              tacc[lv] = fmaf(v1, sdv[jj + 1], tacc[lv]);
-              tc::split_bf16x2(v0, v1, hi[jj / 2], lo[jj / 2]);
+              // two records at a time in the packed f32x2 instructions
+              const unsigned long long v = tc::f2_mul(tc::f2_pack(y[h * 8 + jj], y[h * 8 + jj + 1]),
+                                                      tc::f2_pack(swv[jj], swv[jj + 1]));
+              tacc[lv] = tc::f2_fma(v, tc::f2_pack(sdv[jj], sdv[jj + 1]), tacc[lv]);
+              tc::split_bf16x2_packed(v, hi[jj / 2], lo[jj / 2]);
             }
             const int chunk = gi >> 1, kc = gi & 1;
             const int off_hi = (m >> 3) * 256 + kc * 128 + (m & 7) * 16;
@@ -514,7 +516,10 @@ __global__ void __maxnreg__(128)
         float tv = 0.0f;
 #pragma unroll
         for (int u = 0; u < kG; ++u)
-          if (u == lv) tv = tacc[u];
+          if (u == lv) {
+            const float2 t2 = tc::f2_unpack(tacc[u]);
+            tv = t2.x + t2.y;
+          }
         s_t[q][m] = tv;
         conv_sync();
         if (wq < 2) {

@@ -150,6 +150,43 @@ __device__ inline void split_bf16x2(float v0, float v1, uint32_t& hi, uint32_t& 
   lo = pack_bf16(l0, l1);
 }
 
+// Pairs of FP32 values in one 64-bit register for the packed f32x2 arithmetic
+// of sm_100 and later: one instruction does the work of two FP32 ones.  The
+// low half holds the first value.
+__device__ inline unsigned long long f2_pack(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ inline float2 f2_unpack(unsigned long long v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ inline unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ inline unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                            unsigned long long c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ inline unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+// split_bf16x2 of a packed pair: the same hi and lo, with one packed
+// subtraction for the two residuals
+__device__ inline void split_bf16x2_packed(unsigned long long v, uint32_t& hi, uint32_t& lo) {
+  hi = __byte_perm((uint32_t)v, (uint32_t)(v >> 32), 0x7632);
+  const float2 l = f2_unpack(f2_sub(v, v & 0xffff0000ffff0000ull));
+  lo = pack_bf16(l.x, l.y);
+}
+
 }  // namespace tc
 
 }  // namespace lg

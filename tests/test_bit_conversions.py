@@ -4,7 +4,9 @@ checked against IEEE conversions (numpy): double -> float rounds to nearest,
 ties to even, overflows to infinity, and gives a signed zero below the float
 normal range (where IEEE would give a float subnormal); float -> double is
 exact for normal floats and gives a signed zero for float subnormals.  The
-GPU parity tests of the mixed path cover the device code itself."""
+exact doubling of the QL rotations (twice_bits in csrc/lg_eig2.cu) equals IEEE
+2 x for every double, subnormals, the largest binade, zero, infinity and NaN
+included.  The GPU parity tests cover the device code itself."""
 import struct
 
 import numpy as np
@@ -79,3 +81,31 @@ def test_float_to_double_is_exact_for_normal_floats():
         assert f2d_bits(float(f)) == float(np.float64(f))
     sub = float(np.float32(1e-40))
     assert f2d_bits(sub) == 0.0 and f2d_bits(-sub) == 0.0 and np.signbit(f2d_bits(-sub))
+
+
+def twice_bits(x):
+    u = struct.unpack("<Q", struct.pack("<d", x))[0]
+    sign = u & 0x8000000000000000
+    mag = u ^ sign
+    e = mag >> 52
+    if e == 0:
+        mag <<= 1
+    elif e < 2046:
+        mag += 1 << 52
+    elif e == 2046:
+        mag = 0x7FF0000000000000
+    return struct.unpack("<d", struct.pack("<Q", sign | mag))[0]
+
+
+def test_doubling_on_the_bit_pattern_equals_ieee_doubling():
+    rng = np.random.default_rng(7)
+    xs = rng.standard_normal(20000) * 2.0 ** rng.integers(-1074, 1024, 20000).astype(float)
+    sub = np.array([5e-324, -5e-324, 2.0 ** -1023, 2.0 ** -1022 - 5e-324, -(2.0 ** -1030) * 3])
+    big = np.finfo(np.float64).max
+    edges = np.array([0.0, -0.0, big, -big, big / 2, 2.0 ** 1023, np.inf, -np.inf, 1.0, -3.5])
+    with np.errstate(over="ignore"):
+        for x in np.concatenate([xs, sub, edges]):
+            got = twice_bits(float(x))
+            ref = float(np.float64(x) * 2.0)
+            assert struct.pack("<d", got) == struct.pack("<d", ref), x
+    assert np.isnan(twice_bits(float("nan")))

@@ -96,7 +96,7 @@ struct lg_ctx {
   double lnp_span = 1.0;
   int boff_nb = 0;  // bucket count d_boff was sized for
   // launch shapes and bucket boundaries (lg_set_tuning / lg_autotune)
-  lg_tuning tune{1024, LG_GRAM_AUTO, 128, 1, 4, 4, 0, 0.0};
+  lg_tuning tune{1024, LG_GRAM_AUTO, 512, 2, 4, 4, 0, 0.0};
   // status words: [0] err, [1] eig_fail, [2] nobsl_max, [3] n_capped
   int* d_status = nullptr;
   unsigned long long* d_band = nullptr;

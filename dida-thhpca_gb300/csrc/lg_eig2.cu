@@ -1156,8 +1156,10 @@ void launch_eig2_t(const Geometry& g, const SolveBatch& b, const double* C, cons
     if (ev_tri) record_event(ev_tri, stream);
   }
   if (phases & kEigQL) {
-    // 2. QL, one solve per lane
-    ql_warps = std::max(1, std::min(ql_warps, (int)(kSmemMax / (sizeof(double) * 64 * n))));
+    // 2. QL, one solve per lane; a block takes at most a third of the SM's
+    // shared memory (at 128 members one warp's d and e are 64 KB), so that
+    // three QL blocks, or QL blocks and those of the other streams, share an SM
+    ql_warps = std::max(1, std::min(ql_warps, (int)(kSmemMax / (3 * sizeof(double) * 64 * n))));
     const size_t smem_q = sizeof(double) * (size_t)ql_warps * 64 * n;
     cudaFuncSetAttribute(ql_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_q);
     const int ql_blocks = (ns + 32 * ql_warps - 1) / (32 * ql_warps);

@@ -490,6 +490,13 @@ def main():
         ms = e0.elapsed_time(e1) / args.steps
     clocks = sampler.stop()
     ms, value = job_rate(ms, ncol, world, dev)
+    # the analysis front of the last timed step: H(x), selection and Gram
+    # records before the first chunk's Gram starts (the library's own events)
+    front_ms = None
+    if len(windows) == 1 and not dist:
+        tl = ctx.timeline()
+        if tl.size:
+            front_ms = round(float(tl.reshape(-1, 7)[0, 0]), 2)
     # the timed configuration's analysis, kept for the comparison with plain FP64
     fp64_arm = mixed and not args.no_fp64 and world == 1
     if fp64_arm:
@@ -635,6 +642,9 @@ def main():
         "selection_note": "n_band: candidate pairs with |ri - 2| < 1e-12, where a 1-ulp libm "
                           "difference could flip a list decision; n_eig_fail: eigensolves "
                           "that hit the QL sweep limit",
+        "front_ms": front_ms,
+        "front_note": "ms from the analysis start to the first Gram (H(x) beside the "
+                      "selection, then the Gram records), last timed step",
         "phases_ms": {n: round(v["ms"], 3) for n, v in kernels.items()},
         "phases_note": ("kernel event times of one single-stream analysis (no overlap)"
                         if len(windows) == 1 else

@@ -113,6 +113,9 @@ struct lg_ctx {
   cudaEvent_t ev_io[4] = {};    // lg_run: around the copy in, around the copy out
   std::vector<cudaEvent_t> kev;  // per-launch events of the solve phase
   unsigned long long* d_work = nullptr;
+  // non-zero while the list counts and selection statistics on the device are
+  // those prepare_capacity's count pass just computed for the coming analysis
+  int* d_fresh = nullptr;
   // sizes fixed for the current observation set, and the captured analysis
   bool capacity_ready = false;
   int chunk = 1;
@@ -580,7 +583,8 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   c->y_sec = g.num_lon / g.global_ny;
   c->y_res = g.num_lon % g.global_ny;
   if (dalloc(&c->d_status, 4) != LG_OK || dalloc(&c->d_band, 1) != LG_OK ||
-      dalloc(&c->d_work, 1) != LG_OK) {
+      dalloc(&c->d_work, 1) != LG_OK || dalloc(&c->d_fresh, 1) != LG_OK ||
+      cudaMemset(c->d_fresh, 0, sizeof(int)) != cudaSuccess) {
     lg_destroy(c);
     return LG_ERR_NOMEM;
   }
@@ -1062,12 +1066,22 @@ int prepare_capacity(lg_ctx* c) {
     c->lists.col_list = nullptr;
     c->lists.n_list = 0;
   }
+  // The count pass, with the selection statistics, as the analysis runs it: on
+  // the cell-indexed path the analysis that follows takes these counts and
+  // statistics instead of counting again (d_fresh, cleared by that analysis).
+  const bool cells = c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH");
+  CK(cudaMemsetAsync(c->d_fresh, 0, sizeof(int), st));
   CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
-  if (c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH"))
-    lg::launch_search_cells(geo, c->obs, c->cells, c->lists, 0, nullptr, st);
+  CK(cudaMemsetAsync(c->d_status + 2, 0, sizeof(int) * 2, st));
+  CK(cudaMemsetAsync(c->d_band, 0, sizeof(unsigned long long), st));
+  lg::ListDev lcount = c->lists;
+  lcount.col_stats = c->d_status + 2;  // nobsl_max, n_capped
+  if (cells)
+    lg::launch_search_cells(geo, c->obs, c->cells, lcount, 0, c->d_band, st);
   else
-    lg::launch_search(geo, c->obs, c->lists, 0, nullptr, st);
+    lg::launch_search(geo, c->obs, lcount, 0, c->d_band, st);
   lg::launch_scan_counts(c->lists.cnt, c->lists.off, ncol, c->d_scan_tmp, c->scan_tmp_bytes, st);
+  if (cells) CK(cudaMemsetAsync(c->d_fresh, 1, sizeof(int), st));  // done by the sync below
   CK(cudaGetLastError());
   int64_t total = 0;
   CK(cudaMemcpyAsync(&total, c->lists.off + ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
@@ -1254,11 +1268,14 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   const int ncol = g.num_lat * g.num_lon;
   const int k = g.ens;
   int64_t launches = 0;
-  CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * 4, st));
+  CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * 2, st));  // error, eigensolver failures
   if (phases & kPhaseAnalysis) {
-    CK(cudaMemsetAsync(c->d_band, 0, sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), st));
-    CK(cudaMemsetAsync(c->lists.cnt, 0, sizeof(int) * (ncol + 1), st));
+    // the counts and selection statistics (d_status[2..3], d_band), unless
+    // prepare_capacity has just computed them for this analysis
+    lg::launch_clear_selection(c->d_fresh, c->lists.cnt, ncol + 1, c->d_status + 2, c->d_band,
+                               st);
+    ++launches;
   }
   CK(record_event(c->ev[0], st));
   // H(x) on the side stream, beside the selection on st (the selection needs
@@ -1305,9 +1322,10 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   lg::ListDev lcount = c->lists;
   lcount.col_stats = c->d_status + 2;  // nobsl_max, n_capped
   if (cells)
-    lg::launch_search_cells(geo, c->obs, c->cells, lcount, 0, c->d_band, st);
+    lg::launch_search_cells(geo, c->obs, c->cells, lcount, 0, c->d_band, st, c->d_fresh);
   else
     lg::launch_search(geo, c->obs, lcount, 0, c->d_band, st);
+  CK(cudaMemsetAsync(c->d_fresh, 0, sizeof(int), st));  // later analyses count again
   lg::launch_scan_counts(c->lists.cnt, c->lists.off, ncol, c->d_scan_tmp, c->scan_tmp_bytes, st);
   launches += 3;  // count pass + the scan's init and scan kernels
   if (cells)
@@ -1663,10 +1681,10 @@ int run_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa, dou
   S.n_copies = c->obs.n_copies;
   S.n_entries = c->obs.n_entries;
   S.nobsl_total = analysed ? c->list_total : 0;
-  S.n_band = (int64_t)band;
+  S.n_band = analysed ? (int64_t)band : 0;
   S.n_eig_fail = status[1];
-  S.nobsl_max = status[2];
-  S.n_capped = status[3];
+  S.nobsl_max = analysed ? status[2] : 0;
+  S.n_capped = analysed ? status[3] : 0;
   if (io) {
     S.ms_h2d = elapsed_ms(c->ev_io[0], c->ev_io[1]);
     S.ms_d2h = elapsed_ms(c->ev_io[2], c->ev_io[3]);
@@ -1737,6 +1755,7 @@ int lg_list_counts(lg_ctx* c, int* counts, int64_t* total) {
   lg::ListDev l = c->lists;
   l.col_list = nullptr;  // every column
   l.n_list = 0;
+  CK(cudaMemsetAsync(c->d_fresh, 0, sizeof(int), st));  // the counts are overwritten
   CK(cudaMemsetAsync(l.cnt, 0, sizeof(int) * (ncol + 1), st));
   if (c->have_cells && !getenv("LETKF_GB300_LINEAR_SEARCH"))
     lg::launch_search_cells(c->geo, c->obs, c->cells, l, 0, nullptr, st);
@@ -2196,6 +2215,7 @@ void lg_destroy(lg_ctx* c) {
   if (c->ev_hx) cudaEventDestroy(c->ev_hx);
   for (auto& e : c->kev) cudaEventDestroy(e);
   dfree(c->d_work);
+  dfree(c->d_fresh);
   dfree(c->d_window);
   release_streams(c);
   delete c;

@@ -800,6 +800,19 @@ struct RotBatch {
   __device__ int idx(int j) const { return (int)(((j < 4 ? ix.x : ix.y) >> (8 * (j & 3))) & 0xffu); }
 };
 
+// The log entries of kAheadBatches batches, starting at batch b0 (clipped to
+// the solve's nb batches), into L2 with one bulk prefetch each for the
+// rotations and their indices: issued every kAheadBatches batches, a window
+// ahead of the batch loads, so that those find the entries in L2.
+constexpr int kAheadBatches = 32;  // 256 entries: 2 KB (FP32 log), 4 KB (FP64)
+template <typename LT>
+__device__ inline void prefetch_log(const LT* cs, const unsigned char* ix, int b0, int nb) {
+  const int a = max(b0, 0), e = min(b0 + kAheadBatches, nb);
+  if (e <= a) return;
+  prefetch_l2(cs + (size_t)a * kRotBatch, sizeof(LT) * (size_t)(e - a) * kRotBatch);
+  prefetch_l2(ix + (size_t)a * kRotBatch, (size_t)(e - a) * kRotBatch);
+}
+
 template <typename LT>
 __device__ inline void load_rot_batch(RotBatch<LT>& rb, const LT* cs, const unsigned char* ix,
                                       int b) {
@@ -926,6 +939,7 @@ __global__ void __launch_bounds__(256) __maxnreg__(sizeof(VT) == sizeof(float) ?
     RotBatch<LT> cur, nxt;
     if (nb > 0) load_rot_batch(cur, cs, ix, 0);
     for (int bb = 0; bb < nb; ++bb) {
+      if ((bb & (kAheadBatches - 1)) == 0) prefetch_log(cs, ix, bb + kAheadBatches, nb);
       if (bb + 1 < nb) load_rot_batch(nxt, cs, ix, bb + 1);
 #pragma unroll
       for (int j = 0; j < kRotBatch; ++j) {
@@ -977,6 +991,8 @@ __global__ void __launch_bounds__(256) __maxnreg__(sizeof(VT) == sizeof(float) ?
     RotBatch<LT> cur, nxt;
     if (nb > 0) load_rot_batch(cur, cs, ix, nb - 1);
     for (int bb = nb - 1; bb >= 0; --bb) {
+      if (((nb - 1 - bb) & (kAheadBatches - 1)) == 0)
+        prefetch_log(cs, ix, bb - 2 * kAheadBatches + 1, nb);
       if (bb > 0) load_rot_batch(nxt, cs, ix, bb - 1);
 #pragma unroll
       for (int j = kRotBatch - 1; j >= 0; --j) {

@@ -62,21 +62,6 @@ void launch_obs_trig(const ObsDev& o, double* dcx, double* dsx, double* dyr, flo
                                                                dyr, fcx, fsx, fyr);
 }
 
-// da_vert_coord_calc_ph_lev (x86/DA/utils/vert_coord_mod.F90:547-563), k 1-based
-__device__ inline double calc_ph_lev(const Geometry& g, int k, double phs) {
-  if (g.vcoord == LG_VCOORD_SIGMA)
-    return __dadd_rn(__dmul_rn(g.ca[k - 1], __dsub_rn(phs, g.ptop)), g.ptop);
-  double t1 = __dmul_rn(g.ca[k - 1], __dsub_rn(g.p0, g.ptop));
-  double t2 = __dmul_rn(g.cb[k - 1], __dsub_rn(phs, g.ptop));
-  return __dadd_rn(__dadd_rn(t1, t2), g.ptop);
-}
-
-// half-level pressure ph(j) = 0.5*(ph_lev(j)+ph_lev(j+1)), j = 1..nz, ph(nz+1) = ph(nz)
-__device__ inline double half_ph(const Geometry& g, int j, double ps) {
-  if (j > g.nz) j = g.nz;
-  return __dmul_rn(0.5, __dadd_rn(calc_ph_lev(g, j, ps), calc_ph_lev(g, j + 1, ps)));
-}
-
 // bilinear value (r1*t2 + r2*(1-t2)) of row r at the 2x2 stencil for member e
 __device__ inline double bilin(const double* xb, const double* axb, int k, int n, int e, int r,
                                size_t c11, size_t c21, size_t c12, size_t c22, double t1,
@@ -158,9 +143,34 @@ __global__ void __launch_bounds__(128) hx_kernel(Geometry g, ObsDev ob, const do
   }
   // ph_pos for each obs level; the search index persists across levels
   // (obs_make.F90:252-272).  Levels are processed in order; at most 64 per type.
+  //
+  // The search walks up the member's half levels half_ph(j) = (ph_lev(j) +
+  // ph_lev(j + 1)) / 2 for j = 1..nz (half_ph(nz + 1) = half_ph(nz)).  Each
+  // step needs one new full level: the state of member slot q is its index jj,
+  // b = ph_lev(jj + 1) (jj <= nz), hp = half_ph(jj) and hpm = half_ph(jj - 1)
+  // (jj >= 2), every value formed by the reference's operations in its order,
+  // so the search and the weights below are bit for bit those of evaluating
+  // half_ph afresh at every step.
+  // ph_lev: da_hybrid_coord_calc_ph_lev / da_sigma_coord_calc_ph_lev
+  // (x86/DA/utils/vert_coord_mod.F90:547-563), level kk 1-based
+  const double p0pt = __dsub_rn(g.p0, g.ptop);
+  auto ph_lev = [&](int kk, double psd) -> double {
+    if (g.vcoord == LG_VCOORD_SIGMA) return __dadd_rn(__dmul_rn(g.ca[kk - 1], psd), g.ptop);
+    return __dadd_rn(__dadd_rn(__dmul_rn(g.ca[kk - 1], p0pt), __dmul_rn(g.cb[kk - 1], psd)),
+                     g.ptop);
+  };
   int jj[kMaxMemberSlots];
+  double psd[kMaxMemberSlots], lev_b[kMaxMemberSlots], hp[kMaxMemberSlots],
+      hpm[kMaxMemberSlots];
 #pragma unroll
-  for (int q = 0; q < kMaxMemberSlots; ++q) jj[q] = 1;
+  for (int q = 0; q < kMaxMemberSlots; ++q) {
+    jj[q] = 1;
+    psd[q] = __dsub_rn(ps[q], g.ptop);
+    const double a = ph_lev(1, psd[q]);
+    lev_b[q] = ph_lev(2, psd[q]);
+    hp[q] = __dmul_rn(0.5, __dadd_rn(a, lev_b[q]));
+    hpm[q] = 0.0;
+  }
   bool has3d = false;  // the log-p weights are needed only for 3-D variables
   for (int kv = 0; kv < onv; ++kv) has3d |= g.var_lev[c_types.var[ti][kv]] > 1;
   for (int l = 0; l < onz; ++l) {
@@ -171,12 +181,23 @@ __global__ void __launch_bounds__(128) hx_kernel(Geometry g, ObsDev ob, const do
     for (int q = 0; q < kMaxMemberSlots; ++q) {
       const int e = (int)lane + 32 * q;
       if (e < k) {
-        while (jj[q] <= g.nz && po > half_ph(g, jj[q], ps[q])) jj[q]++;
+        // while (jj <= nz && po > half_ph(jj)) jj++; half_ph(nz + 1) is
+        // half_ph(nz), so hp needs no update when jj reaches nz + 1
+        while (jj[q] <= g.nz && po > hp[q]) {
+          hpm[q] = hp[q];
+          ++jj[q];
+          if (jj[q] <= g.nz) {
+            const double a = lev_b[q];
+            lev_b[q] = ph_lev(jj[q] + 1, psd[q]);
+            hp[q] = __dmul_rn(0.5, __dadd_rn(a, lev_b[q]));
+          }
+        }
       }
       pp[q] = jj[q] - 1;
     }
     // vertical interpolation weight in log p of each member for this level,
-    // shared by the level's variables
+    // shared by the level's variables: with p = jj - 1 in [1, nz), half_ph(p + 1)
+    // is hp and half_ph(p) is hpm
     double t3[kMaxMemberSlots];
 #pragma unroll
     for (int q = 0; q < kMaxMemberSlots; ++q) {
@@ -184,9 +205,8 @@ __global__ void __launch_bounds__(128) hx_kernel(Geometry g, ObsDev ob, const do
       const int p = pp[q];
       t3[q] = 0.0;
       if (has3d && e < k && p >= 1 && p < g.nz) {
-        const double php1 = half_ph(g, p + 1, ps[q]), php = half_ph(g, p, ps[q]);
-        const double lp1 = log(php1);
-        t3[q] = __ddiv_rn(__dsub_rn(lp1, lnpo), __dsub_rn(lp1, log(php)));
+        const double lp1 = log(hp[q]);
+        t3[q] = __ddiv_rn(__dsub_rn(lp1, lnpo), __dsub_rn(lp1, log(hpm[q])));
       }
     }
     for (int kv = 0; kv < onv; ++kv) {

@@ -180,8 +180,16 @@ void launch_hx_import(int ens, int64_t e0, int64_t e1, HxDev hx, const double* r
                       cudaStream_t stream);
 void launch_search(const Geometry& g, const ObsDev& o, ListDev l, int fill,
                    unsigned long long* band, cudaStream_t stream);
+// skip (count pass only, may be null): when *skip is non-zero the launch does
+// nothing -- the counts and statistics are already those of this selection
 void launch_search_cells(const Geometry& g, const ObsDev& o, const CellIndex& ci, ListDev l,
-                         int fill, unsigned long long* band, cudaStream_t stream);
+                         int fill, unsigned long long* band, cudaStream_t stream,
+                         const int* skip = nullptr);
+// zero the selection's counts (n ints), its two statistics and the band
+// counter, unless *fresh is non-zero (the count pass that sized the lists has
+// just computed them for the same columns and observations)
+void launch_clear_selection(const int* fresh, int* cnt, int n, int* col_stats,
+                            unsigned long long* band, cudaStream_t stream);
 void launch_scan_counts(const int* cnt, int64_t* off, int n, void* tmp, size_t tmp_bytes,
                         cudaStream_t stream);
 size_t scan_tmp_bytes(int n);

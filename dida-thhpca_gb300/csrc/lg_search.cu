@@ -17,6 +17,8 @@
 #include <cuda/std/functional>
 #include <cub/device/device_scan.cuh>
 
+#include <algorithm>
+
 #include "lg_device.cuh"
 #include "lg_internal.h"
 
@@ -193,12 +195,24 @@ __global__ void __launch_bounds__(128) records_kernel(int col0, int ncol, ListDe
     if (i < p) atomicAdd(&cur[bucket(l.ent[base + i]) + 1], 1);
   }
   __syncwarp();
-  // exclusive scan over buckets (one lane; nb is small)
-  if (lane == 0) {
-    int acc = 0;
-    for (int b = 0; b <= nb; ++b) {
+  // cur[b] <- first record of bucket b (the scan of the shifted counts): each
+  // lane scans a run of consecutive buckets from the total of the runs before
+  // it, which a shuffle scan over the warp provides
+  {
+    const int run = (nb + 32) / 32;  // ceil((nb + 1) / 32)
+    const int b0 = min(nb + 1, lane * run), b1 = min(nb + 1, b0 + run);
+    int sum = 0;
+    for (int b = b0; b < b1; ++b) sum += cur[b];
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    int acc = incl - sum;
+    for (int b = b0; b < b1; ++b) {
       acc += cur[b];
-      cur[b] = acc;  // cur[b] = first record of bucket b
+      cur[b] = acc;
     }
   }
   __syncwarp();
@@ -308,7 +322,9 @@ __device__ inline float schr2_f32(float ri) {
 
 __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob, CellIndex ci,
                                                            ListDev l, int fill, SearchArgs sa,
-                                                           unsigned long long* band) {
+                                                           unsigned long long* band,
+                                                           const int* skip) {
+  if (skip && *skip) return;
   const int warps = blockDim.x / 32;
   const int w = threadIdx.x >> 5;
   const int idx = blockIdx.x * warps + w;
@@ -487,7 +503,8 @@ __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob
 }
 
 void launch_search_cells(const Geometry& g, const ObsDev& o, const CellIndex& ci, ListDev l,
-                         int fill, unsigned long long* band, cudaStream_t stream) {
+                         int fill, unsigned long long* band, cudaStream_t stream,
+                         const int* skip) {
   const int ncol = g.num_lat * g.num_lon;
   const double th = 2.0 * g.local_dist / earth_r4();
   SearchArgs sa;
@@ -506,7 +523,25 @@ void launch_search_cells(const Geometry& g, const ObsDev& o, const CellIndex& ci
   const int nc = l.col_list ? l.n_list : ncol;
   if (nc == 0) return;
   search_cells_kernel<<<(nc + warps - 1) / warps, 32 * warps, smem, stream>>>(g, o, ci, l, fill,
-                                                                                 sa, band);
+                                                                                 sa, band, skip);
+}
+
+__global__ void clear_selection_kernel(const int* fresh, int* cnt, int n, int* col_stats,
+                                       unsigned long long* band) {
+  if (*fresh) return;
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) cnt[i] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    col_stats[0] = 0;
+    col_stats[1] = 0;
+    *band = 0ull;
+  }
+}
+
+void launch_clear_selection(const int* fresh, int* cnt, int n, int* col_stats,
+                            unsigned long long* band, cudaStream_t stream) {
+  const int blocks = std::max(1, std::min((n + 255) / 256, 152 * 4));
+  clear_selection_kernel<<<blocks, 256, 0, stream>>>(fresh, cnt, n, col_stats, band);
 }
 
 }  // namespace lg

@@ -215,3 +215,47 @@ def test_repeated_runs_replay_the_captured_graph():
         ctx.letkf_final()
     finally:
         del os.environ["LETKF_GB300_NO_GRAPH"]
+
+
+def test_first_analysis_takes_the_sizing_counts():
+    """After lg_set_obs the first analysis takes the neighbour-list counts and
+    selection statistics of the count pass that sized the lists; later analyses
+    count again.  Lists, statistics and analyses must agree bit for bit, for a
+    second observation set and back, in both precisions."""
+    import letkf_gb300 as lg
+    import synth
+
+    keys = ("nobsl_total", "nobsl_max", "n_capped", "n_band")
+    for prec in (lg.LG_PREC_FP64, lg.LG_PREC_MIXED):
+        cfg = lg.preset("small3d").replace(max_obs=40, precision=prec)
+        w = synth.make_workload(cfg)
+        o = w.obs
+        m = o.n_obs // 2
+        half = lg.ObsSet(o.types, o.type[:m], o.lat[:m], o.lon[:m], o.ph[:m], o.yo[:m],
+                         o.rinv[:m])
+
+        def run(ctx):
+            xa = np.zeros_like(w.xb)
+            axa = np.zeros_like(w.axb)
+            ctx.letkf_run(0, w.xb, w.axb, xa, axa)
+            st = ctx.stats()
+            return xa, axa, ctx.lists(), {k: st[k] for k in keys}
+
+        def same(a, b):
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+            for x, y in zip(a[2], b[2]):
+                assert np.array_equal(x, y)
+            assert a[3] == b[3], (a[3], b[3])
+
+        ctx = lg.Letkf(cfg)
+        ctx.set_obs(o)
+        first = run(ctx)
+        same(first, run(ctx))
+        assert first[3]["n_capped"] > 0 and first[3]["nobsl_max"] == 40
+        ctx.set_obs(half)
+        h1 = run(ctx)
+        same(h1, run(ctx))
+        assert h1[3]["nobsl_total"] < first[3]["nobsl_total"]
+        ctx.set_obs(o)
+        same(run(ctx), first)
+        ctx.letkf_final()

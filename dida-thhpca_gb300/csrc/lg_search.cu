@@ -320,6 +320,21 @@ __device__ inline float schr2_f32(float ri) {
   return 1.0f;
 }
 
+// cos of a longitude difference x in (-3 pi, 3 pi) radians for the FP32
+// prefilter: x reduced to [-pi, pi] by the nearest multiple of the FP32 2 pi
+// (error below 3e-7 for these x), then the hardware approximation __cosf
+// (absolute error 2^-21.41 on [-pi, pi], CUDA Programming Guide, intrinsic
+// functions).  The prefilter decides only candidates whose FP32 cosine of the
+// angular distance is more than 1e-5 from the threshold's (the band between
+// SearchArgs::vlo and vhi goes to the exact FP64 test), and this cosine and
+// the FP32 products around it are off by less than 1e-6, so every decision is
+// the exact test's.
+__device__ inline float cos_prefilter(float x) {
+  const float k2pi = 6.28318530717958648f;
+  const float r = x - k2pi * rintf(x * (1.0f / k2pi));
+  return __cosf(r);
+}
+
 __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob, CellIndex ci,
                                                            ListDev l, int fill, SearchArgs sa,
                                                            unsigned long long* band,
@@ -407,7 +422,7 @@ __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob
               pos = perm[i];
               const float4 cd = cand[i];
               if (cd.w != 0.0f) {  // within obs_polar
-                const float v32 = cd.x * fcx * cosf(cd.z - fyr) + cd.y * fsx;
+                const float v32 = cd.x * fcx * cos_prefilter(cd.z - fyr) + cd.y * fsx;
                 if (v32 > sa.vhi) {
                   keep = true;
                 } else if (v32 >= sa.vlo) {  // in the band: the exact FP64 test

@@ -85,6 +85,10 @@ struct lg_ctx {
   cudaStream_t side_stream = nullptr, third_stream = nullptr, fourth_stream = nullptr;
   cudaStream_t copy_stream = nullptr;  // lg_run: host copies beside the analysis
   cudaEvent_t ev_copy_in = nullptr, ev_copy_join = nullptr;
+  // lg_run: the background comes in by longitude pieces, one event after each
+  // (H(x) of a group of longitude blocks waits only for the pieces it reads)
+  static constexpr int kCopyPieces = 4;
+  cudaEvent_t ev_piece[kCopyPieces] = {};
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join3 = nullptr, ev_join4 = nullptr;
   // [Gram, tridiagonalisation (or eigensolve), QL, vectors done][buffer set]
   cudaEvent_t ev_phase[4][4] = {};
@@ -355,6 +359,11 @@ void release_streams(lg_ctx* c) {
       cudaEventDestroy(*ep);
       *ep = nullptr;
     }
+  for (auto& e : c->ev_piece)
+    if (e) {
+      cudaEventDestroy(e);
+      e = nullptr;
+    }
   for (auto& row : c->ev_phase)
     for (auto& e : row)
       if (e) {
@@ -542,6 +551,8 @@ int lg_create(lg_ctx** out, const lg_config* cfg) {
   for (auto& row : c->ev_phase)
     for (auto& e : row)
       made = made && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  for (auto& e : c->ev_piece)
+    made = made && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
   if (!made) {
     cudaGetLastError();
     release_streams(c);
@@ -1282,29 +1293,82 @@ int enqueue_analysis(lg_ctx* c, const double* xb, const double* axb, double* xa,
   // only observation positions; the records and Grams wait for H(x))
   CK(cudaEventRecord(c->ev_fork, st));
   CK(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
+  // Copy pieces of the background (lg_run with host arrays, the whole globe's
+  // H(x)): up to kCopyPieces groups of longitude blocks; piece p holds the
+  // longitudes up to group p's last one + 1, in whole rows of the
+  // [lon + 2 halo] arrays, and each row's bytes are a multiple of 16 (the copy
+  // kernel's unit).  One piece otherwise.
+  const int lon_e = g.num_lon + 2 * g.halo;
+  int npiece = 1;
+  size_t piece_row[lg_ctx::kCopyPieces + 1] = {0, (size_t)lon_e};
+  int piece_by[lg_ctx::kCopyPieces + 1] = {0, g.global_ny};
+  if (io && (phases & kPhaseHx) && !own_copies) {
+    const size_t row_x = sizeof(double) * (size_t)(g.num_lat + 2 * g.halo) * c->geo.n * k;
+    const size_t row_a = sizeof(double) * (size_t)(g.num_lat + 2 * g.halo) * c->geo.n;
+    const int np = std::min(lg_ctx::kCopyPieces, g.global_ny);
+    if (np > 1 && row_x % 16 == 0 && row_a % 16 == 0) {
+      npiece = np;
+      for (int p = 0; p <= np; ++p) piece_by[p] = (int)((int64_t)g.global_ny * p / np);
+      piece_row[0] = 0;
+      for (int p = 1; p < np; ++p) {
+        // last longitude (1-based) of the group's last block, then + 1 and the halo
+        const int e_lon = c->blk[(size_t)(piece_by[p] - 1) * g.global_nx].w;
+        piece_row[p] = std::min<size_t>((size_t)lon_e, (size_t)e_lon + 1 + g.halo);
+      }
+      piece_row[np] = (size_t)lon_e;
+    }
+  }
   if (io) {
     // the background in, on the copy stream; H(x) (and everything after it) waits
     const size_t cols = (size_t)(g.num_lat + 2 * g.halo) * (g.num_lon + 2 * g.halo);
     CK(cudaStreamWaitEvent(c->copy_stream, c->ev_fork, 0));
     CK(record_event(c->ev_io[0], c->copy_stream));
     const size_t bx = sizeof(double) * cols * c->geo.n * k, ba = sizeof(double) * cols * c->geo.n;
-    if (io->xb_map && io->axb_map) {
-      CK(lg::launch_copy_mapped(io->xb_map, (void*)xb, bx, c->copy_stream));
-      CK(lg::launch_copy_mapped(io->axb_map, (void*)axb, ba, c->copy_stream));
-      launches += 2;
-    } else {
-      CK(cudaMemcpyAsync((void*)xb, io->xb, bx, cudaMemcpyHostToDevice, c->copy_stream));
-      CK(cudaMemcpyAsync((void*)axb, io->axb, ba, cudaMemcpyHostToDevice, c->copy_stream));
+    // rows (longitudes with the halo) of the xb and axb arrays per copy piece
+    const size_t rx = bx / lon_e, ra = ba / lon_e;
+    for (int p = 0; p < npiece; ++p) {
+      const size_t r0 = piece_row[p], r1 = piece_row[p + 1];
+      if (io->xb_map && io->axb_map) {
+        CK(lg::launch_copy_mapped(io->xb_map + r0 * rx / 8, (double*)xb + r0 * rx / 8,
+                                  (r1 - r0) * rx, c->copy_stream));
+        CK(lg::launch_copy_mapped(io->axb_map + r0 * ra / 8, (double*)axb + r0 * ra / 8,
+                                  (r1 - r0) * ra, c->copy_stream));
+        launches += 2;
+      } else {
+        CK(cudaMemcpyAsync((double*)xb + r0 * rx / 8, io->xb + r0 * rx / 8, (r1 - r0) * rx,
+                           cudaMemcpyHostToDevice, c->copy_stream));
+        CK(cudaMemcpyAsync((double*)axb + r0 * ra / 8, io->axb + r0 * ra / 8, (r1 - r0) * ra,
+                           cudaMemcpyHostToDevice, c->copy_stream));
+      }
+      if (npiece > 1) CK(cudaEventRecord(c->ev_piece[p], c->copy_stream));
     }
     CK(record_event(c->ev_io[1], c->copy_stream));
     CK(cudaEventRecord(c->ev_copy_in, c->copy_stream));
-    CK(cudaStreamWaitEvent(c->side_stream, c->ev_copy_in, 0));
+    if (npiece == 1) CK(cudaStreamWaitEvent(c->side_stream, c->ev_copy_in, 0));
   }
   if (phases & kPhaseHx) {
     int64_t j0 = 0, j1 = c->obs.n_copies, e0 = 0, e1 = 0;
     if (own_copies) shard_copies(c, &j0, &j1, &e0, &e1);
-    lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, c->side_stream, j0, j1);
-    launches += j1 > j0;
+    if (io && npiece > 1) {
+      // H(x) of longitude-block group p after copy piece p, which ends at the
+      // group's last longitude + 1 (the stencil's eastern column); the pieces
+      // before it are in by then
+      for (int p = 0; p < npiece; ++p) {
+        CK(cudaStreamWaitEvent(c->side_stream, c->ev_piece[p], 0));
+        const std::vector<int>& cb = c->h_copy_block;
+        const int64_t a = std::lower_bound(cb.begin(), cb.end(), piece_by[p] * g.global_nx) -
+                          cb.begin();
+        const int64_t b = std::lower_bound(cb.begin(), cb.end(), piece_by[p + 1] * g.global_nx) -
+                          cb.begin();
+        lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, c->side_stream, a, b);
+        launches += b > a;
+      }
+      // everything after H(x) (records, Grams, updates) reads the whole background
+      CK(cudaStreamWaitEvent(c->side_stream, c->ev_copy_in, 0));
+    } else {
+      lg::launch_hx(geo, c->obs, xb, axb, c->hx, c->d_status, c->side_stream, j0, j1);
+      launches += j1 > j0;
+    }
   }
   CK(record_event(c->ev[1], c->side_stream));
   CK(cudaEventRecord(c->ev_hx, c->side_stream));

@@ -185,8 +185,11 @@ __global__ void __launch_bounds__(128) records_kernel(int col0, int ncol, ListDe
   __syncwarp();
   const int64_t base = l.off[col];
   const int p = l.cnt[col];
+  // FP64 -> FP32 by integer operations (d2f_bits: round to nearest even, as the
+  // conversion instruction, which issues on the FP64 pipe; magnitudes below
+  // 2^-126 become zero): four conversions per list entry
   auto bucket = [&](int ent) {
-    int b = (int)floorf(((float)hx.lnp[ent] - lo) * inv_dz);
+    int b = (int)floorf((d2f_bits(hx.lnp[ent]) - lo) * inv_dz);
     return b < 0 ? 0 : (b >= nb ? nb - 1 : b);
   };
   // histogram
@@ -234,8 +237,8 @@ __global__ void __launch_bounds__(128) records_kernel(int col0, int ncol, ListDe
     __syncwarp();
     if (ok) {
       const int64_t pos = base + start + rank;
-      rec[pos] = make_float4(__int_as_float(ent), (float)hx.lnp[ent],
-                             hx.rdiag[ent] * (float)l.rloc[base + i], (float)hx.dis[ent]);
+      rec[pos] = make_float4(__int_as_float(ent), d2f_bits(hx.lnp[ent]),
+                             hx.rdiag[ent] * d2f_bits(l.rloc[base + i]), d2f_bits(hx.dis[ent]));
     }
     if (ok && rank == 0) cur[b] = start + __popc(same);
     __syncwarp();
@@ -485,7 +488,7 @@ __global__ void __launch_bounds__(128) search_cells_kernel(Geometry g, ObsDev ob
           } else {  // mixed path: the weight only needs FP32 accuracy
             const float v32 = fminf(ob.fcx[o] * fcx * cosf(ob.fyr[o] - fyr) + ob.fsx[o] * fsx, 1.0f);
             const float ri = fminf(6371.393f * acosf(v32) / (float)g.local_dist, 2.0f);
-            gc = (double)(g.gc_filter ? schr2_f32(ri) : 1.0f);
+            gc = f2d_bits(g.gc_filter ? schr2_f32(ri) : 1.0f);  // off the FP64 pipe
           }
           const int e0 = ob.copy_eoff[j];
           int64_t posw = written + (int64_t)t * nent;

@@ -331,7 +331,8 @@ typedef struct lg_tuning {
   int gram_kernel; /* LG_GRAM_* (mixed precision) */
   int lnp_buckets; /* ln p buckets of the Gram records (mixed, vertical localisation), 8..1024:
                       the bucket boundaries that bound each level's record window */
-  int ql_warps;    /* warps per block of the QL kernel, 1..6 */
+  int ql_warps;    /* warps per block of the QL kernel, 1..6; a block takes at most a third
+                      of an SM's shared memory (at most 2 warps at 64 members, 1 above) */
   int vec_warps;   /* warps per block of the vector/update kernel, 1..8 */
   int solve_streams; /* 1; 2: chunks alternate between two streams with their own scratch;
                         3: phase pipeline (Grams, eigensolves, vector updates on three

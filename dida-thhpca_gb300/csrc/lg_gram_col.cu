@@ -141,10 +141,18 @@ __device__ inline bool wait(uint64_t* bar, uint32_t parity, volatile int* abort,
   }
 }
 
-// ln p of level kk (1-based) at column col and its window [w0, w1) of records
-__device__ inline void level_window(const Geometry& g, const ListDev& l, const RecDev& rec,
-                                    const double* axb, int col, int kk, float& al, int& w0,
-                                    int& w1) {
+// ln p of level kk (1-based) at column col and its window [w0, w1) of records.
+// The producer, MMA and converter warps each compute an item's windows, and
+// they must agree to the bit: a window one record stage wider in one role than
+// in another leaves the roles waiting for each other.  The function is
+// therefore compiled once (not inlined): inlined copies of its FP32
+// expressions can be contracted into fused multiply-adds differently at each
+// call site, and with 512 ln p buckets such a difference crossed a bucket
+// boundary on the clustered 2e6-observation workload and the Gram's waits ran
+// out.
+__device__ __noinline__ void level_window(const Geometry& g, const ListDev& l,
+                                          const RecDev& rec, const double* axb, int col, int kk,
+                                          float& al, int& w0, int& w1) {
   w0 = 0;
   w1 = l.cnt[col];
   al = 0.0f;

@@ -726,9 +726,12 @@ __global__ void __launch_bounds__(256) ql_kernel(int n, int nsolves, double shif
 // vector, so one load per rotation would leave the chain waiting on DRAM at
 // every step.  The log is therefore read kRotBatch entries at a time, one batch
 // ahead of the rotations that use it (the loads of a batch are independent and
-// in flight together), and every load asks L2 for the whole 256-byte segment
-// around it, so that the following entries are found there.  The data are
-// read-only for the kernel (non-coherent loads).
+// in flight together); every load asks L2 for the whole 256-byte segment
+// around it, and a bulk prefetch every kAheadBatches batches brings the next
+// window of entries into L2 (prefetch_log).  The reflector block of a solve is
+// prefetched into L2 before each Householder pass and its step flags read once
+// (load_step_mask).  The data are read-only for the kernel (non-coherent
+// loads).
 constexpr int kRotBatch = 8;
 
 template <typename LT>
@@ -758,9 +761,8 @@ __device__ inline double ld_stream<double>(const double* p) {
   return v;
 }
 
-// One bulk prefetch into L2 of the 16-byte-aligned interior of [p, p + bytes):
-// a solve's reflector block, just before a Householder pass reads it step by
-// step (each step's loads would otherwise wait on DRAM in turn).
+// One bulk prefetch into L2 of the 16-byte-aligned interior of [p, p + bytes)
+// (a solve's reflector block, or a window of its rotation log).
 __device__ inline void prefetch_l2(const void* p, size_t bytes) {
   const size_t a0 = __cvta_generic_to_global(p);
   const size_t a = (a0 + 15) & ~(size_t)15, e = (a0 + bytes) & ~(size_t)15;

@@ -6,7 +6,8 @@ normal range (where IEEE would give a float subnormal); float -> double is
 exact for normal floats and gives a signed zero for float subnormals.  The
 exact doubling of the QL rotations (twice_bits in csrc/lg_eig2.cu) equals IEEE
 2 x for every double, subnormals, the largest binade, zero, infinity and NaN
-included.  The GPU parity tests cover the device code itself."""
+included, and the selection prefilter's argument reduction keeps its cosine
+within 3e-7.  The GPU parity tests cover the device code itself."""
 import struct
 
 import numpy as np
@@ -109,3 +110,25 @@ def test_doubling_on_the_bit_pattern_equals_ieee_doubling():
             ref = float(np.float64(x) * 2.0)
             assert struct.pack("<d", got) == struct.pack("<d", ref), x
     assert np.isnan(twice_bits(float("nan")))
+
+
+def test_prefilter_argument_reduction_error():
+    """The selection prefilter's cosine (cos_prefilter in csrc/lg_search.cu)
+    reduces a longitude difference x in (-3 pi, 3 pi) to [-pi, pi] by the
+    nearest multiple of the FP32 2 pi, in FP32 without contraction (the file is
+    built with -fmad=false): restated in numpy float32, the cosine of the
+    reduced argument is within 3e-7 of the cosine of x, and the argument lies
+    in [-pi, pi] up to rounding, where the hardware cosine's documented error
+    bound holds; both stay far inside the 1e-5 band that goes to the exact
+    FP64 test."""
+    k2pi = np.float32(6.28318530717958648)
+    inv = np.float32(1.0) / k2pi
+    rng = np.random.default_rng(11)
+    x = rng.uniform(-3 * np.pi, 3 * np.pi, 200000).astype(np.float32)
+    x = np.concatenate([x, np.float32([0.0, np.pi, -np.pi, 2 * np.pi, -2 * np.pi, 3 * np.pi - 1e-3])])
+    n = np.rint(x * inv).astype(np.float32)
+    r = (x - (k2pi * n).astype(np.float32)).astype(np.float32)
+    exact = np.remainder(x.astype(np.float64) + np.pi, 2 * np.pi) - np.pi
+    err = np.abs(np.cos(r.astype(np.float64)) - np.cos(exact))
+    assert err.max() < 3e-7, err.max()
+    assert np.all(np.abs(r) <= np.float32(np.pi) * (1 + 1e-6))
